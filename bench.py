@@ -1,0 +1,313 @@
+"""Benchmark of the D2Q9 step: GLUPS and the fraction of the HBM roofline.
+
+Workload (one GPU): the plain FP32 channel -- 4096 x 4096 cells, Zou-He parabolic inlet
+(peak u = 0.05), zero-gradient outflow, bounce-back walls top and bottom, seeded
+non-overlapping disks (radius U[8, 32], 5 % solid), tau = 0.56, equilibrium start.  A
+bench step is one LBM time step over the whole lattice.  The working set (2 x 604 MB of
+populations) is larger than L2, so no flush is needed between steps.
+
+Output: one JSON line.  value = cell updates / s / 1e9 over the timed steps (device time,
+CUDA events on the library's stream); e2e = the same metric for the whole job through the
+public API (create from host parameters, mask built and uploaded from the host, K steps,
+macro field read back to host memory); roofline = 72 algorithmic bytes per cell update
+over the measured HBM copy bandwidth; cpu_baseline = the oracle (the CPU restatement of
+the reference path) on the host cores for a bounded sample.
+
+--impl reference times that CPU restatement alone (all host threads), the reference
+having no CPU implementation of its own (its path is WGSL run by wgpu, which needs a
+graphics API these machines do not have).
+
+Multi-GPU: replicas only -- each rank advances its own copy of the workload; no
+collectives touch the data path.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_VALUE = {"f32": 4, "f16": 2, "bf16": 2, "f64": 8}  # 9 loads + 9 stores per cell update
+METRIC = "D2Q9 GLUPS (FP32 channel 4096^2), % HBM roofline"
+UNIT = "GLUPS"
+
+
+def workload_params(args):
+    return dict(nx=args.nx, ny=args.ny, mode="physics", dtype=args.dtype, scene="channel", tau=0.56,
+                inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0), seed=1234)
+
+
+def config_dict(args):
+    return {"workload": "channel %dx%d %s, Zou-He inlet u=0.05 parabolic, outflow, walls, disks r 8-32 5%% solid, "
+                        "tau 0.56, equilibrium start" % (args.nx, args.ny, args.dtype),
+            "cells": args.nx * args.ny, "steps_per_bench_step": 1, "l2_flush": "none: working set 1.2 GB > L2",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "channel_step_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_sample(args, seconds_cap=12.0):
+    """The oracle's FP32 physics step on a 4096-wide slice of the channel, all host threads."""
+    import numpy as np
+
+    import oracle
+
+    ny = max(64, min(args.ny, int(os.environ.get("LBM_CPU_SAMPLE_ROWS", "512"))))
+    info, _ = oracle.mask_physics_channel(args.nx, ny, 0.05, 1234, 0.05, 8.0, 32.0)
+    sim = oracle.PhysOracle(info, 0.56, np.float32)
+    sim.step(2)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        sim.step(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > seconds_cap or steps >= 200:
+            break
+    glups = args.nx * ny * steps / el / 1e9
+    return {"value": glups, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": "oracle FP32 physics step on a %dx%d slice of the channel workload, %d steps, %.1f s"
+                      % (args.nx, ny, steps, el)}
+
+
+def run_reference(args):
+    """CPU restatement of the reference path (oracle), each step a bounded slice."""
+    import numpy as np
+
+    import oracle
+
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    ny = max(64, min(args.ny, int(os.environ.get("LBM_CPU_SAMPLE_ROWS", "512"))))
+    info, _ = oracle.mask_physics_channel(args.nx, ny, 0.05, 1234, 0.05, 8.0, 32.0)
+    sim = oracle.PhysOracle(info, 0.56, np.float32)
+    sim.step(args.warmup)
+    t0 = time.perf_counter()
+    sim.step(args.steps)
+    el = time.perf_counter() - t0
+    glups = args.nx * ny * args.steps / el / 1e9
+    cores = oracle.num_threads()
+    line = {"impl": "reference", "metric": METRIC, "value": glups, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded channel mask)", "config": config_dict(args),
+            "cpu_baseline": {"value": glups, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "oracle FP32 physics step on a %dx%d slice of the channel workload per step"
+                                       % (args.nx, ny)},
+            "e2e": {"value": glups, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    from simuverse_gb300 import FluidSimulator
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    params = workload_params(args)
+    cells = args.nx * args.ny
+    sim = FluidSimulator(**params)
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.step(args.warmup)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, device time on the launching stream
+    clocks = ClockSampler(local)
+    clocks.start()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    launches0 = sim.kernel_launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sim.step(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    ms = ev0.elapsed_time(ev1)
+    gpu_launches = sim.kernel_launches - launches0
+    clk = clocks.stop()
+    ms_max = ms
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * cells * args.steps / (ms_max * 1e-3) / 1e9
+    per_launch_s = ms * 1e-3 / args.steps
+    bytes_per_cell = 18 * BYTES_PER_VALUE[args.dtype]
+    achieved = bytes_per_cell * cells / per_launch_s / 1e9
+    peak, peak_kind = measured_peak()
+    tr = committed_traffic()
+
+    # ---- macro every step (the reference's behaviour), reported separately
+    sim_m = FluidSimulator(macro_every_step=True, **params)
+    sim_m.set_stream(stream.cuda_stream)
+    sim_m.step(args.warmup)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sim_m.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    glups_macro = cells * args.steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    sim_m.close()
+    sim.close()
+    torch.cuda.synchronize()
+
+    # ---- end to end through the public API, host buffers
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s2 = FluidSimulator(**params)
+    s2.step(args.steps)
+    rho, ux, uy = s2.read_macro()
+    t_e2e = time.perf_counter() - t0
+    s2.close()
+    assert np.isfinite(rho).all()
+    e2e_glups = cells * args.steps / t_e2e / 1e9
+    if pg:
+        t = torch.tensor([t_e2e], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_glups = world * cells * args.steps / float(t.item()) / 1e9
+    h2d = cells * 16  # info records uploaded at creation
+    d2h = cells * 12  # rho, ux, uy read back
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+            "data": "synthetic (seeded channel mask, equilibrium start)", "config": config_dict(args),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": (tr or {}).get("bytes_per_launch_scaled"),
+                         "traffic_source": (tr or {}).get("source"),
+                         "algorithmic_bytes_per_launch": bytes_per_cell * cells},
+            "macro_every_step_glups": glups_macro,
+            "e2e": {"value": e2e_glups, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps,
+                    "what": "create (host mask build + upload) + K steps + macro read-back, wall clock"},
+            "gpu_launches": gpu_launches,
+            "clocks": clk,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_sample(args)
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=4096)
+    ap.add_argument("--ny", type=int, default=4096)
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,208 @@
+/*
+ * lbm.h -- C ABI of the GB300-native D2Q9 lattice-Boltzmann library (liblbm.so).
+ *
+ * This is the drop-in boundary for simuverse's fluid path.  Each entry point names the
+ * reference interface it replaces (paths inside the simuverse project):
+ *
+ *   lbm_create            FluidSimulator::new      simuverse/src/fluid/fluid_simulator.rs:26-133
+ *                         D2Q9Node::new            simuverse/src/fluid/d2q9_node.rs:31-209
+ *   lbm_step              D2Q9Node::compute_by_pass simuverse/src/fluid/d2q9_node.rs:302-312
+ *   lbm_compute           Simulator::compute       simuverse/src/fluid/fluid_simulator.rs:217-232
+ *   lbm_reset             Simulator::reset         simuverse/src/fluid/fluid_simulator.rs:210-215
+ *                         D2Q9Node::reset_lattice_info simuverse/src/fluid/d2q9_node.rs:247-261
+ *   lbm_set_tau /
+ *   lbm_update_viscosity  Simulator::update_uniforms simuverse/src/fluid/fluid_simulator.rs:175-193
+ *   lbm_on_click          Simulator::on_click      simuverse/src/fluid/fluid_simulator.rs:137-152
+ *   lbm_add_obstacle      D2Q9Node::add_obstacle   simuverse/src/fluid/d2q9_node.rs:215-245
+ *   lbm_touch_begin       Simulator::touch_begin   simuverse/src/fluid/fluid_simulator.rs:154-156
+ *   lbm_touch_move        Simulator::touch_move    simuverse/src/fluid/fluid_simulator.rs:158-173
+ *   lbm_add_external_force D2Q9Node::add_external_force simuverse/src/fluid/d2q9_node.rs:263-300
+ *   lbm_read_macro /
+ *   lbm_read_macro_rgba16f the macro_tex the step writes  assets/wgsl/lbm/collide_stream.wgsl:36,74
+ *   lbm_set_info/get_info the info buffer            simuverse/src/fluid/lattice.rs:5-24
+ *
+ * The remaining entry points (populations, conservation sums, checkpoints, the batched
+ * form) have no counterpart in the reference; each says so.
+ *
+ * Conventions.  Every function returns an int status (LBM_OK = 0, negative on error,
+ * LBM_IGNORED = 1 when the reference would silently ignore the request) and never
+ * aborts; lbm_last_error() gives the message of the calling thread's last failure.
+ * Host arrays are plain pointers owned by the caller.  Work is queued on the handle's
+ * CUDA stream and the read functions synchronise that stream.  One handle must not be
+ * used from two threads at once.
+ *
+ * Layout.  Cell (x, y) is x + y*nx with y growing downwards (screen rows, as in the
+ * reference).  Populations are structure-of-arrays: direction i of cell c at c + i*N,
+ * N = nx*ny (assets/wgsl/lbm/d2q9_fn.wgsl:13-17).  Direction order, vectors and
+ * inverses follow simuverse/src/fluid/mod.rs:39-52:
+ *   0:(0,0) 1:(1,0) 2:(0,-1) 3:(-1,0) 4:(0,1) 5:(1,-1) 6:(-1,-1) 7:(-1,1) 8:(1,1)
+ */
+#ifndef SIMUVERSE_GB300_LBM_H
+#define SIMUVERSE_GB300_LBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_ABI_VERSION 1
+
+/* status codes */
+#define LBM_OK 0
+#define LBM_IGNORED 1
+#define LBM_ERR_ARG (-1)
+#define LBM_ERR_CUDA (-2)
+#define LBM_ERR_TIMEOUT (-3)
+#define LBM_ERR_NAN (-4)
+#define LBM_ERR_IO (-5)
+#define LBM_ERR_STATE (-6)
+#define LBM_ERR_NOMEM (-7)
+
+/* step rules */
+#define LBM_MODE_REFERENCE 0 /* the reference's shaders exactly: truncated weights, clamps,
+                                forcing rows, wall-cell storage bounce-back */
+#define LBM_MODE_PHYSICS 1   /* exact weights, no clamps, half-way bounce-back with moving
+                                walls, Zou-He west inlet, zero-gradient east outflow */
+
+/* population storage */
+#define LBM_DTYPE_F32 0  /* reference mode: absolute f_i; physics mode: f_i - w_i */
+#define LBM_DTYPE_F64 1  /* physics mode only: f_i - w_i in FP64, FP64 arithmetic */
+#define LBM_DTYPE_F16 2  /* physics mode only: (f_i - w_i) * 2^10 in FP16, FP32 arithmetic */
+#define LBM_DTYPE_BF16 3 /* physics mode only: f_i - w_i in BF16, FP32 arithmetic */
+
+/* initial masks */
+#define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */
+#define LBM_SCENE_CAVITY 1     /* lattice.rs:52-61 (reference); moving-lid box (physics) */
+#define LBM_SCENE_CUSTOM 2     /* lattice.rs:47-51: box walls */
+#define LBM_SCENE_CHANNEL 3    /* physics: walls y=0 and y=ny-1, parabolic Zou-He inlet at
+                                  x=0, outflow at x=nx-1, seeded non-overlapping disks */
+#define LBM_SCENE_PERIODIC 4   /* physics: no walls, periodic on both axes */
+
+/* materials: lattice.rs:15-24 */
+#define LBM_BULK 1
+#define LBM_BOUNDARY 2
+#define LBM_INLET 3
+#define LBM_OBSTACLE 4
+#define LBM_OUTLET 5
+#define LBM_EXTERNAL_FORCE 6
+#define LBM_GHOST 7
+
+/* per-cell record, byte-compatible with LatticeInfo (lattice.rs:5-13) */
+typedef struct lbm_lattice_info {
+    int32_t material;
+    int32_t block_iter; /* forcing countdown; -1 = permanent */
+    float vx;           /* forcing / wall / inlet velocity */
+    float vy;
+} lbm_lattice_info;
+
+typedef struct lbm_params {
+    int32_t nx, ny;          /* lattice size (D2Q9Node::new derives it from the canvas) */
+    int32_t mode;            /* LBM_MODE_* */
+    int32_t dtype;           /* LBM_DTYPE_* */
+    int32_t scene;           /* LBM_SCENE_* */
+    float tau;               /* relaxation time; omega = 1/tau (mod.rs:32-36) */
+    float lid_speed;         /* cavity lid velocity; reference literal 0.13 (lattice.rs:58) */
+    float inlet_speed;       /* Poiseuille forcing 0.12 (lattice.rs:69); channel peak inlet u */
+    float solid_fraction;    /* channel: solid fraction of the seeded disks */
+    float disk_rmin, disk_rmax; /* channel: disk radius range (cells) */
+    uint64_t seed;           /* channel: disk placement seed (mt19937_64) */
+    int32_t pixel_size;      /* canvas pixels per lattice cell for on_click/touch_move */
+    int32_t macro_every_step;/* 1: write the macro field every step, as the reference does;
+                                0: only on the last step of each lbm_step call */
+    int32_t reserved[6];
+} lbm_params;
+
+typedef struct lbm_handle lbm_handle;
+
+/* library */
+int lbm_abi_version(void);
+const char* lbm_last_error(void);
+void lbm_params_default(lbm_params* p);
+
+/* lifetime -- FluidSimulator::new / drop */
+int lbm_create(const lbm_params* p, lbm_handle** out);
+int lbm_destroy(lbm_handle* h);
+/* run the handle's work on a caller-owned cudaStream_t (NULL restores its own stream);
+   no counterpart in the reference */
+int lbm_set_stream(lbm_handle* h, void* cuda_stream);
+int lbm_get_size(const lbm_handle* h, int32_t* nx, int32_t* ny);
+int lbm_get_params(const lbm_handle* h, lbm_params* out);
+
+/* stepping -- D2Q9Node::compute_by_pass (one call = collide+stream+boundary) */
+int lbm_step(lbm_handle* h, int32_t nsteps);
+/* Simulator::compute: one frame = two steps (swap 0 then 1) */
+int lbm_compute(lbm_handle* h);
+/* Simulator::reset / D2Q9Node::reset_lattice_info */
+int lbm_reset(lbm_handle* h);
+/* Simulator::update_uniforms: tau = 3*viscosity + 0.5 */
+int lbm_update_viscosity(lbm_handle* h, float viscosity);
+int lbm_set_tau(lbm_handle* h, float tau);
+
+/* interaction -- Simulator::on_click / touch_begin / touch_move; canvas pixel coordinates */
+int lbm_on_click(lbm_handle* h, float px, float py);
+int lbm_add_obstacle(lbm_handle* h, int32_t x, int32_t y);
+int lbm_touch_begin(lbm_handle* h);
+int lbm_touch_move(lbm_handle* h, float px, float py);
+int lbm_add_external_force(lbm_handle* h, float pos_x, float pos_y, float pre_x, float pre_y);
+
+/* host-only mask helpers (no GPU needed; the handle functions above use the same code).
+   lbm_build_mask: the scene mask of p (init_lattice_material, lattice.rs:26-98, for the
+   reference scenes).  lbm_mask_add_obstacle: the disc of D2Q9Node::add_obstacle applied to a
+   host array (rows y-28 .. y+27).  lbm_mask_force_stroke: the cells and record that
+   D2Q9Node::add_external_force writes; it returns the number of cells written. */
+int lbm_build_mask(const lbm_params* p, lbm_lattice_info* out);
+int lbm_mask_add_obstacle(int32_t nx, int32_t ny, lbm_lattice_info* info, int32_t x, int32_t y);
+int lbm_mask_force_stroke(int32_t nx, int32_t ny, int32_t pixel_size, lbm_lattice_info* info, float pos_x,
+                          float pos_y, float pre_x, float pre_y);
+
+/* mask -- the info buffer (N records).  set_info replaces both the device buffer and the
+   host copy that add_obstacle uploads rows from. */
+int lbm_set_info(lbm_handle* h, const lbm_lattice_info* info);
+int lbm_get_info(lbm_handle* h, lbm_lattice_info* out);
+
+/* fields -- macro_tex (collide_stream.wgsl:36,74): rho (clamped in reference mode),
+   ux, uy of the last step; walls give 0.  Any pointer may be NULL. */
+int lbm_read_macro(lbm_handle* h, float* rho, float* ux, float* uy);
+/* the rgba16float texel (ux, uy, rho, 1) / (0,0,0,0) on walls, as IEEE half bits */
+int lbm_read_macro_rgba16f(lbm_handle* h, uint16_t* rgba);
+
+/* populations -- no counterpart in the reference (its buffers are GPU-private).
+   Absolute f_i as FP32 (dst_dtype LBM_DTYPE_F32) or FP64 (LBM_DTYPE_F64), 9*N values,
+   the state the next step reads. */
+int lbm_read_populations(lbm_handle* h, void* dst, int32_t dst_dtype);
+int lbm_write_populations(lbm_handle* h, const void* src, int32_t src_dtype);
+/* physics mode: equilibrium at (rho, ux, uy) host arrays of N floats (NULL: rho=1, u=0) */
+int lbm_init_equilibrium(lbm_handle* h, const float* rho, const float* ux, const float* uy);
+
+/* diagnostics -- no counterpart in the reference.  FP64 sums over non-solid cells of
+   the absolute populations: out[0] mass, out[1] x momentum, out[2] y momentum;
+   deterministic (fixed reduction order). */
+int lbm_conservation(lbm_handle* h, double out[3]);
+/* number of non-finite populations; returns LBM_ERR_NAN when it is not zero */
+int lbm_check_finite(lbm_handle* h, uint64_t* count);
+/* relative L2 errors of this handle's last macro field against ref's (same size):
+   out[0] = |rho - rho_ref|_2 / |rho_ref|_2, out[1] = |u - u_ref|_2 / |u_ref|_2,
+   out[2] = max |u - u_ref|, out[3] = max |rho - rho_ref| (FP64 sums over non-solid cells) */
+int lbm_macro_error(lbm_handle* h, lbm_handle* ref, double out[4]);
+
+/* checkpoint -- no counterpart in the reference.  Header (magic, version, nx, ny, mode,
+   dtype, scene, tau, steps), then the raw state buffer, the info records and the host
+   copy of the info records. */
+int lbm_save(lbm_handle* h, const char* path);
+int lbm_load(lbm_handle* h, const char* path);
+
+/* counters -- no counterpart in the reference */
+int lbm_steps_done(const lbm_handle* h, uint64_t* steps);
+int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches);
+
+/* device views for in-GPU consumers (particles, colour mapping); valid until destroy.
+   macro: 3 planes of N floats (rho, ux, uy).  No counterpart in the reference, whose
+   consumers bind macro_tex directly. */
+int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

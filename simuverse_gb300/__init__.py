@@ -1,0 +1,9 @@
+"""GB300-native D2Q9 lattice-Boltzmann step (simuverse's fluid path) over liblbm.so.
+
+``FluidSimulator`` mirrors simuverse's fluid simulator API; the compute runs in the
+hand-written sm_103a kernels of ``csrc/`` behind the C ABI of ``include/lbm.h``.
+"""
+from ._native import INFO_DTYPE, LbmError, load  # noqa: F401
+from .fluid import FluidSimulator  # noqa: F401
+
+__all__ = ["FluidSimulator", "LbmError", "INFO_DTYPE", "load"]

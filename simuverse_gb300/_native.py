@@ -1,0 +1,134 @@
+"""ctypes binding of liblbm.so (include/lbm.h).
+
+The library must have been built (``simuverse_gb300.build.build()`` or
+``__graft_entry__.build()``); there is no fallback implementation, and loading fails
+loudly when the shared object is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liblbm.so")
+
+# status codes (lbm.h)
+LBM_OK = 0
+LBM_IGNORED = 1
+LBM_ERR_ARG = -1
+LBM_ERR_CUDA = -2
+LBM_ERR_TIMEOUT = -3
+LBM_ERR_NAN = -4
+LBM_ERR_IO = -5
+LBM_ERR_STATE = -6
+LBM_ERR_NOMEM = -7
+
+MODES = {"reference": 0, "physics": 1}
+DTYPES = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
+SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4}
+BULK, BOUNDARY, INLET, OBSTACLE, OUTLET, EXTERNAL_FORCE, GHOST = 1, 2, 3, 4, 5, 6, 7
+
+# LatticeInfo (simuverse/src/fluid/lattice.rs:5-13)
+INFO_DTYPE = np.dtype([("material", "<i4"), ("block_iter", "<i4"), ("vx", "<f4"), ("vy", "<f4")])
+
+
+class LbmParams(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+        ("mode", ctypes.c_int32), ("dtype", ctypes.c_int32), ("scene", ctypes.c_int32),
+        ("tau", ctypes.c_float), ("lid_speed", ctypes.c_float), ("inlet_speed", ctypes.c_float),
+        ("solid_fraction", ctypes.c_float), ("disk_rmin", ctypes.c_float), ("disk_rmax", ctypes.c_float),
+        ("seed", ctypes.c_uint64),
+        ("pixel_size", ctypes.c_int32), ("macro_every_step", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
+    ]
+
+
+class LbmError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__("lbm error %d: %s" % (code, message))
+        self.code = code
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int32
+_F = ctypes.c_float
+_D = ctypes.c_double
+
+# name -> argtypes; every function returns int
+_SIGNATURES = {
+    "lbm_create": [ctypes.POINTER(LbmParams), ctypes.POINTER(_P)],
+    "lbm_destroy": [_P],
+    "lbm_set_stream": [_P, _P],
+    "lbm_get_size": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)],
+    "lbm_get_params": [_P, ctypes.POINTER(LbmParams)],
+    "lbm_step": [_P, _I],
+    "lbm_compute": [_P],
+    "lbm_reset": [_P],
+    "lbm_update_viscosity": [_P, _F],
+    "lbm_set_tau": [_P, _F],
+    "lbm_on_click": [_P, _F, _F],
+    "lbm_add_obstacle": [_P, _I, _I],
+    "lbm_touch_begin": [_P],
+    "lbm_touch_move": [_P, _F, _F],
+    "lbm_add_external_force": [_P, _F, _F, _F, _F],
+    "lbm_build_mask": [ctypes.POINTER(LbmParams), _P],
+    "lbm_mask_add_obstacle": [_I, _I, _P, _I, _I],
+    "lbm_mask_force_stroke": [_I, _I, _I, _P, _F, _F, _F, _F],
+    "lbm_set_info": [_P, _P],
+    "lbm_get_info": [_P, _P],
+    "lbm_read_macro": [_P, _P, _P, _P],
+    "lbm_read_macro_rgba16f": [_P, _P],
+    "lbm_read_populations": [_P, _P, _I],
+    "lbm_write_populations": [_P, _P, _I],
+    "lbm_init_equilibrium": [_P, _P, _P, _P],
+    "lbm_conservation": [_P, ctypes.POINTER(_D)],
+    "lbm_check_finite": [_P, ctypes.POINTER(ctypes.c_uint64)],
+    "lbm_macro_error": [_P, _P, ctypes.POINTER(_D)],
+    "lbm_save": [_P, ctypes.c_char_p],
+    "lbm_load": [_P, ctypes.c_char_p],
+    "lbm_steps_done": [_P, ctypes.POINTER(ctypes.c_uint64)],
+    "lbm_kernel_launches": [_P, ctypes.POINTER(ctypes.c_uint64)],
+    "lbm_device_macro": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)],
+}
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load liblbm.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("liblbm.so is missing at %s: build it with simuverse_gb300.build.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.lbm_abi_version.restype = ctypes.c_int
+    lib.lbm_abi_version.argtypes = []
+    lib.lbm_last_error.restype = ctypes.c_char_p
+    lib.lbm_last_error.argtypes = []
+    lib.lbm_params_default.restype = None
+    lib.lbm_params_default.argtypes = [ctypes.POINTER(LbmParams)]
+    for name, args in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = ctypes.c_int
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int) -> int:
+    """Raise LbmError for a negative status; return the status otherwise."""
+    if code < 0:
+        msg = load().lbm_last_error().decode(errors="replace")
+        raise LbmError(code, msg)
+    return code
+
+
+def ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def exported_symbols():
+    """Names declared in include/lbm.h that the library must export."""
+    return ["lbm_abi_version", "lbm_last_error", "lbm_params_default"] + list(_SIGNATURES)

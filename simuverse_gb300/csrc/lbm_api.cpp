@@ -1,0 +1,784 @@
+// lbm_api.cpp -- the C ABI of include/lbm.h: handle lifetime, masks, interactive edits,
+// read-back, diagnostics and checkpoints.  Host logic mirrors simuverse's fluid module:
+//   D2Q9Node::new                simuverse/src/fluid/d2q9_node.rs:31-209
+//   init_lattice_material        simuverse/src/fluid/lattice.rs:26-98
+//   D2Q9Node::add_obstacle       simuverse/src/fluid/d2q9_node.rs:215-245
+//   D2Q9Node::reset_lattice_info simuverse/src/fluid/d2q9_node.rs:247-261
+//   D2Q9Node::add_external_force simuverse/src/fluid/d2q9_node.rs:263-300
+//   FluidSimulator::on_click / touch_move / update_uniforms
+//                                simuverse/src/fluid/fluid_simulator.rs:137-193
+// Built with -ffp-contract=off so that the float geometry of the masks and force strokes
+// rounds as the Rust code does.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "lbm_internal.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define LBM_CK(call)                                                                                 \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(LBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define LBM_TRY(expr)          \
+    do {                       \
+        int r_ = (expr);       \
+        if (r_ < 0) return r_; \
+    } while (0)
+
+constexpr float OBSTACLE_RADIUS = 28.0f;  // fluid/mod.rs:1
+
+bool sd_sphere(float px, float py, float r) {  // fluid/mod.rs:57-59 (glam Vec2::length)
+    const float d = std::sqrt(px * px + py * py);
+    return d <= r;
+}
+
+lbm_lattice_info make_info(int material, float vx = 0.0f, float vy = 0.0f, int block_iter = -1) {
+    lbm_lattice_info r;
+    r.material = material;
+    r.block_iter = block_iter;
+    r.vx = vx;
+    r.vy = vy;
+    return r;
+}
+
+// lattice.rs:26-98 (nz = 1)
+void mask_reference(int nx, int ny, int scene, float lid, float inlet, std::vector<lbm_lattice_info>& out) {
+    out.resize((size_t)nx * ny);
+    const float s0x = (float)nx / 7.0f - OBSTACLE_RADIUS, s0y = (float)ny / 2.0f;
+    const float s1x = (float)nx / 5.0f, s1y = (float)ny / 4.0f;
+    const float s2x = (float)nx / 5.0f, s2y = (float)ny * 0.75f;
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            int m = LBM_BULK;
+            float vx = 0.0f;
+            if (scene == LBM_SCENE_CUSTOM) {
+                if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) m = LBM_BOUNDARY;
+            } else if (scene == LBM_SCENE_CAVITY) {
+                if (x == 0 || x == nx - 1 || y == ny - 1) m = LBM_BOUNDARY;
+                else if (y == 0) m = LBM_GHOST;
+                else if (y == 1) { m = LBM_EXTERNAL_FORCE; vx = lid; }
+            } else {  // Poiseuille
+                if (y == 0 || y == ny - 1) m = LBM_BOUNDARY;
+                else if (x == 0 || x == nx - 1) m = LBM_GHOST;
+                else if (x == 1) { m = LBM_INLET; vx = inlet; }
+                else if (x == nx - 2) m = LBM_OUTLET;
+                else {
+                    const float px = (float)x, py = (float)y;
+                    if (sd_sphere(px - s0x, py - s0y, OBSTACLE_RADIUS) || sd_sphere(px - s1x, py - s1y, OBSTACLE_RADIUS) ||
+                        sd_sphere(px - s2x, py - s2y, OBSTACLE_RADIUS))
+                        m = LBM_OBSTACLE;
+                }
+            }
+            out[(size_t)y * nx + x] = make_info(m, vx);
+        }
+}
+
+// physics-mode lid-driven cavity: solid box, row y = 0 (screen top) moves with lid_vx
+void mask_phys_cavity(int nx, int ny, float lid, std::vector<lbm_lattice_info>& out) {
+    out.resize((size_t)nx * ny);
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            const bool wall = x == 0 || x == nx - 1 || y == 0 || y == ny - 1;
+            const float vx = (y == 0 && x >= 1 && x <= nx - 2) ? lid : 0.0f;
+            out[(size_t)y * nx + x] = make_info(wall ? LBM_BOUNDARY : LBM_BULK, vx);
+        }
+}
+
+double unit53(std::mt19937_64& g) { return (double)(g() >> 11) * (1.0 / 9007199254740992.0); }
+
+// Channel: walls y = 0 and y = ny-1, Zou-He inlet x = 0 with the parabolic profile of a
+// channel whose walls sit half-way between rows, outflow x = nx-1, and non-overlapping
+// disks (radius U[rmin, rmax], gap >= 2 cells) placed by rejection sampling until the
+// solid fraction is reached.  Returns the number of disks.
+int mask_phys_channel(int nx, int ny, float u_max, uint64_t seed, float frac, float rmin, float rmax,
+                      std::vector<lbm_lattice_info>& out) {
+    out.resize((size_t)nx * ny);
+    const double H = (double)(ny - 2);
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            lbm_lattice_info r = make_info(LBM_BULK);
+            if (y == 0 || y == ny - 1) r.material = LBM_BOUNDARY;
+            else if (x == 0) {
+                r.material = LBM_INLET;
+                const double s = (double)y - 0.5;
+                r.vx = (float)(4.0 * (double)u_max * s * (H - s) / (H * H));
+            } else if (x == nx - 1) r.material = LBM_OUTLET;
+            out[(size_t)y * nx + x] = r;
+        }
+    const long target = (long)std::ceil((double)frac * (double)nx * (double)ny);
+    const double xlo = nx / 16 > 2 ? (double)(nx / 16) : 2.0;
+    const double xhi = (double)(nx - 1) - (nx / 8 > 2 ? (double)(nx / 8) : 2.0);
+    const double ylo = 2.0, yhi = (double)(ny - 3);
+    std::mt19937_64 g(seed);
+    std::vector<double> disks;
+    long solid = 0, attempts = 0;
+    while (solid < target && attempts < 200000) {
+        ++attempts;
+        const double r = (double)rmin + ((double)rmax - (double)rmin) * unit53(g);
+        const double u2 = unit53(g), u3 = unit53(g);
+        if (xhi - xlo < 2.0 * r || yhi - ylo < 2.0 * r) continue;
+        const double cx = xlo + r + (xhi - xlo - 2.0 * r) * u2;
+        const double cy = ylo + r + (yhi - ylo - 2.0 * r) * u3;
+        bool ok = true;
+        for (size_t k = 0; k < disks.size(); k += 3) {
+            const double dx = cx - disks[k], dy = cy - disks[k + 1], md = r + disks[k + 2] + 2.0;
+            if (dx * dx + dy * dy < md * md) { ok = false; break; }
+        }
+        if (!ok) continue;
+        disks.push_back(cx); disks.push_back(cy); disks.push_back(r);
+        const int x0 = (int)std::floor(cx - r), x1 = (int)std::ceil(cx + r);
+        const int y0 = (int)std::floor(cy - r), y1 = (int)std::ceil(cy + r);
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                if (x < 1 || x > nx - 2 || y < 1 || y > ny - 2) continue;
+                const double dx = (double)x - cx, dy = (double)y - cy;
+                if (dx * dx + dy * dy <= r * r) {
+                    lbm_lattice_info& c = out[(size_t)y * nx + x];
+                    if (c.material != LBM_OBSTACLE) { c.material = LBM_OBSTACLE; ++solid; }
+                }
+            }
+    }
+    return (int)(disks.size() / 3);
+}
+
+void build_scene_mask(const lbm_params& p, std::vector<lbm_lattice_info>& out) {
+    if (p.mode == LBM_MODE_REFERENCE) {
+        mask_reference(p.nx, p.ny, p.scene, p.lid_speed, p.inlet_speed, out);
+        return;
+    }
+    switch (p.scene) {
+        case LBM_SCENE_CAVITY: mask_phys_cavity(p.nx, p.ny, p.lid_speed, out); break;
+        case LBM_SCENE_CHANNEL:
+            mask_phys_channel(p.nx, p.ny, p.inlet_speed, p.seed, p.solid_fraction, p.disk_rmin, p.disk_rmax, out);
+            break;
+        case LBM_SCENE_PERIODIC: out.assign((size_t)p.nx * p.ny, make_info(LBM_BULK)); break;
+        default: mask_reference(p.nx, p.ny, p.scene, p.lid_speed, p.inlet_speed, out); break;
+    }
+}
+
+// d2q9_node.rs:222-241: cells of rows [y-28, y+28) within radius 28 of (x+0.5, y+0.5)
+void obstacle_disc(int nx, int x, int y, lbm_lattice_info* info) {
+    const int r = (int)OBSTACLE_RADIUS;
+    const int min_y = y - r, max_y = min_y + 2 * r;
+    const float cx = (float)x + 0.5f, cy = (float)y + 0.5f;
+    for (int yy = min_y; yy < max_y; ++yy)
+        for (int xx = 0; xx < nx; ++xx)
+            if (sd_sphere((float)xx + 0.5f - cx, (float)yy + 0.5f - cy, OBSTACLE_RADIUS))
+                info[(size_t)yy * nx + xx] = make_info(LBM_OBSTACLE);
+}
+
+// d2q9_node.rs:269-299: the record and the cells (in stroke order) of a force stroke
+lbm_lattice_info force_stroke(int nx, int ny, int pixel_size, float pos_x, float pos_y, float pre_x, float pre_y,
+                              std::vector<size_t>& cells) {
+    const float ddx = pos_x - pre_x, ddy = pos_y - pre_y;
+    const float dis = std::sqrt(ddx * ddx + ddy * ddy);
+    float force = 0.1f * (dis / 20.0f);
+    if (force > 0.12f) force = 0.12f;
+    const float ridian = std::atan2(pos_y - pre_y, pos_x - pre_x);
+    const float vx = force * std::cos(ridian);
+    const float vy = force * std::sin(ridian);
+    const float c = std::ceil(dis / (float)(pixel_size - 1));
+    const float step = dis / c;
+    const int count = (int)c;
+    const unsigned ps = (unsigned)pixel_size;
+    for (int i = 0; i < count; ++i) {
+        const float d = step * (float)i;
+        const float p_x = std::round(pre_x + d * std::cos(ridian));
+        const float p_y = std::round(pre_y + d * std::sin(ridian));
+        const unsigned ux = p_x <= 0.0f ? 0u : (unsigned)p_x;  // Rust `as u32` saturates
+        const unsigned uy = p_y <= 0.0f ? 0u : (unsigned)p_y;
+        const unsigned x = ux / ps, y = uy / ps;
+        if (x < 1 || (long)x >= (long)nx - 2 || y < 1 || (long)y >= (long)ny - 2) continue;
+        cells.push_back((size_t)y * nx + x);
+    }
+    return make_info(LBM_EXTERNAL_FORCE, vx, vy, 90);
+}
+
+int validate_params(const lbm_params& p) {
+    if (p.nx < 4 || p.ny < 4 || p.nx > 65535 || p.ny > 65535)
+        return fail(LBM_ERR_ARG, "lattice %dx%d outside [4, 65535]", p.nx, p.ny);
+    if ((size_t)p.nx * (size_t)p.ny > ((size_t)1 << 30))
+        return fail(LBM_ERR_ARG, "lattice of %zu cells exceeds 2^30", (size_t)p.nx * p.ny);
+    if (p.mode != LBM_MODE_REFERENCE && p.mode != LBM_MODE_PHYSICS) return fail(LBM_ERR_ARG, "unknown mode %d", p.mode);
+    if (p.dtype < LBM_DTYPE_F32 || p.dtype > LBM_DTYPE_BF16) return fail(LBM_ERR_ARG, "unknown dtype %d", p.dtype);
+    if (p.mode == LBM_MODE_REFERENCE && p.dtype != LBM_DTYPE_F32)
+        return fail(LBM_ERR_ARG, "reference mode stores FP32 populations only");
+    if (p.scene < 0 || p.scene > LBM_SCENE_PERIODIC) return fail(LBM_ERR_ARG, "unknown scene %d", p.scene);
+    if (p.mode == LBM_MODE_REFERENCE && p.scene > LBM_SCENE_CUSTOM)
+        return fail(LBM_ERR_ARG, "scene %d exists in physics mode only", p.scene);
+    if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
+    if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
+    if (p.scene == LBM_SCENE_CHANNEL && !(p.disk_rmin >= 0.0f && p.disk_rmax >= p.disk_rmin && p.solid_fraction >= 0.0f &&
+                                         p.solid_fraction < 0.5f))
+        return fail(LBM_ERR_ARG, "channel disk parameters out of range");
+    return LBM_OK;
+}
+
+int use_device(const lbm_handle* h) {
+    LBM_CK(cudaSetDevice(h->device));
+    return LBM_OK;
+}
+
+int upload_info_rows(lbm_handle* h, int y0, int y1) {
+    const size_t off = (size_t)y0 * h->nx, cnt = (size_t)(y1 - y0) * h->nx;
+    LBM_CK(cudaMemcpyAsync(h->d_info + off, h->host_info.data() + off, cnt * sizeof(lbm_lattice_info),
+                           cudaMemcpyHostToDevice, h->stream));
+    return LBM_OK;
+}
+
+int rebuild_flags(lbm_handle* h) {
+    LBM_CK(lbm::launch_build_flags(h, h->stream));
+    ++h->launches;
+    return LBM_OK;
+}
+
+int init_state(lbm_handle* h) {
+    if (h->p.mode == LBM_MODE_REFERENCE) {
+        LBM_CK(lbm::launch_ref_init(h, h->stream));
+    } else {
+        LBM_CK(lbm::launch_phys_init(h, nullptr, nullptr, nullptr, h->stream));
+    }
+    ++h->launches;
+    h->cur = 0;
+    h->stepped_since_init = false;
+    return LBM_OK;
+}
+
+int sync(lbm_handle* h) {
+    LBM_CK(cudaStreamSynchronize(h->stream));
+    return LBM_OK;
+}
+
+void free_all(lbm_handle* h) {
+    cudaFree(h->buf[0]);
+    cudaFree(h->buf[1]);
+    cudaFree(h->d_flags);
+    cudaFree(h->d_info);
+    cudaFree(h->d_macro);
+    cudaFree(h->d_part);
+    cudaFree(h->d_count);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+int check_handle(const lbm_handle* h) {
+    if (!h) return fail(LBM_ERR_ARG, "null handle");
+    return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_abi_version(void) { return LBM_ABI_VERSION; }
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+
+void lbm_params_default(lbm_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->nx = 600;  // 1200x750 canvas at lattice_pixel_size 2 (app_handler.rs:57-58, d2q9_node.rs:38-43)
+    p->ny = 375;
+    p->mode = LBM_MODE_REFERENCE;
+    p->dtype = LBM_DTYPE_F32;
+    p->scene = LBM_SCENE_POISEUILLE;
+    p->tau = 3.0f * 0.02f + 0.5f;  // setting_obj.rs:32 viscosity 0.02
+    p->lid_speed = 0.13f;
+    p->inlet_speed = 0.12f;
+    p->solid_fraction = 0.05f;
+    p->disk_rmin = 8.0f;
+    p->disk_rmax = 32.0f;
+    p->seed = 0;
+    p->pixel_size = 2;
+    p->macro_every_step = 0;
+}
+
+int lbm_create(const lbm_params* pin, lbm_handle** out) {
+    if (!pin || !out) return fail(LBM_ERR_ARG, "null argument");
+    *out = nullptr;
+    const lbm_params& p = *pin;
+    LBM_TRY(validate_params(p));
+
+    lbm_handle* h = new (std::nothrow) lbm_handle();
+    if (!h) return fail(LBM_ERR_NOMEM, "out of host memory");
+    h->p = p;
+    h->nx = p.nx;
+    h->ny = p.ny;
+    h->N = (size_t)p.nx * p.ny;
+    h->fluid_ty = (p.scene == LBM_SCENE_CAVITY) ? 1 : 0;
+    h->tau = p.tau;
+    h->omega = 1.0f / p.tau;
+    cudaError_t e = cudaGetDevice(&h->device);
+    const size_t pop_bytes = 9 * h->N * lbm::dtype_size(p.dtype);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    h->stream = h->own_stream;
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf[0], pop_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&h->buf[1], pop_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_flags, h->N * sizeof(uint16_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_info, h->N * sizeof(lbm_lattice_info));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_macro, 3 * h->N * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_part, (size_t)lbm::RED_BLOCKS * 6 * sizeof(double) + 64 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_count, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        free_all(h);
+        delete h;
+        return fail(LBM_ERR_CUDA, "allocation for a %dx%d lattice failed: %s", p.nx, p.ny, cudaGetErrorString(e));
+    }
+    build_scene_mask(p, h->host_info);
+    int r = upload_info_rows(h, 0, h->ny);
+    if (r == LBM_OK) r = rebuild_flags(h);
+    if (r == LBM_OK) r = init_state(h);
+    if (r == LBM_OK) r = sync(h);
+    if (r != LBM_OK) {
+        free_all(h);
+        delete h;
+        return r;
+    }
+    *out = h;
+    return LBM_OK;
+}
+
+int lbm_destroy(lbm_handle* h) {
+    if (!h) return LBM_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return LBM_OK;
+}
+
+int lbm_set_stream(lbm_handle* h, void* s) {
+    LBM_TRY(check_handle(h));
+    LBM_TRY(use_device(h));
+    LBM_CK(cudaStreamSynchronize(h->stream));
+    h->stream = s ? (cudaStream_t)s : h->own_stream;
+    return LBM_OK;
+}
+
+int lbm_get_size(const lbm_handle* h, int32_t* nx, int32_t* ny) {
+    LBM_TRY(check_handle(h));
+    if (nx) *nx = h->nx;
+    if (ny) *ny = h->ny;
+    return LBM_OK;
+}
+
+int lbm_get_params(const lbm_handle* h, lbm_params* out) {
+    LBM_TRY(check_handle(h));
+    if (!out) return fail(LBM_ERR_ARG, "null output");
+    *out = h->p;
+    out->tau = h->tau;
+    return LBM_OK;
+}
+
+int lbm_step(lbm_handle* h, int32_t nsteps) {
+    LBM_TRY(check_handle(h));
+    if (nsteps < 0) return fail(LBM_ERR_ARG, "negative step count");
+    LBM_TRY(use_device(h));
+    for (int32_t s = 0; s < nsteps; ++s) {
+        const bool macro = h->p.macro_every_step || s == nsteps - 1;
+        LBM_CK(lbm::launch_step(h, macro, h->stream));
+        h->cur ^= 1;
+        ++h->steps;
+        ++h->launches;
+    }
+    if (nsteps > 0) h->stepped_since_init = true;
+    return LBM_OK;
+}
+
+int lbm_compute(lbm_handle* h) { return lbm_step(h, 2); }
+
+int lbm_reset(lbm_handle* h) {
+    LBM_TRY(check_handle(h));
+    LBM_TRY(use_device(h));
+    // reference: only the Poiseuille scene rebuilds its mask (d2q9_node.rs:248-255)
+    if (h->p.mode == LBM_MODE_PHYSICS || h->p.scene == LBM_SCENE_POISEUILLE) {
+        build_scene_mask(h->p, h->host_info);
+        LBM_TRY(upload_info_rows(h, 0, h->ny));
+    }
+    LBM_TRY(rebuild_flags(h));
+    LBM_TRY(init_state(h));
+    h->pre_x = h->pre_y = 0.0f;  // fluid_simulator.rs:214
+    return sync(h);
+}
+
+int lbm_set_tau(lbm_handle* h, float tau) {
+    LBM_TRY(check_handle(h));
+    if (!(tau > 0.0f) || !std::isfinite(tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
+    h->tau = tau;
+    h->omega = 1.0f / tau;  // mod.rs:35
+    return LBM_OK;
+}
+
+int lbm_update_viscosity(lbm_handle* h, float viscosity) {
+    const float tau = 3.0f * viscosity + 0.5f;  // fluid_simulator.rs:177
+    return lbm_set_tau(h, tau);
+}
+
+int lbm_add_obstacle(lbm_handle* h, int32_t x, int32_t y) {
+    LBM_TRY(check_handle(h));
+    const int r = (int)OBSTACLE_RADIUS;
+    const int min_y = y - r, max_y = min_y + 2 * r;
+    if (x < 0 || x >= h->nx || min_y < 0 || max_y > h->ny)
+        return fail(LBM_ERR_ARG, "obstacle rows [%d, %d) or column %d outside the lattice", min_y, max_y, x);
+    LBM_TRY(use_device(h));
+    obstacle_disc(h->nx, x, y, h->host_info.data());
+    // the reference uploads whole rows from its host copy (d2q9_node.rs:243-244)
+    LBM_TRY(upload_info_rows(h, min_y, max_y));
+    LBM_TRY(rebuild_flags(h));
+    return sync(h);
+}
+
+int lbm_on_click(lbm_handle* h, float px, float py) {
+    LBM_TRY(check_handle(h));
+    if (px <= 0.0f || py <= 0.0f) return LBM_IGNORED;
+    const unsigned ps = (unsigned)h->p.pixel_size;
+    const unsigned x = (unsigned)px / ps, y = (unsigned)py / ps;
+    const unsigned half = (unsigned)OBSTACLE_RADIUS;
+    if (x < half || (long)x >= (long)h->nx - (long)(half + 2) || y < half || (long)y >= (long)h->ny - (long)(half + 2))
+        return LBM_IGNORED;
+    return lbm_add_obstacle(h, (int32_t)x, (int32_t)y);
+}
+
+int lbm_touch_begin(lbm_handle* h) {
+    LBM_TRY(check_handle(h));
+    h->pre_x = h->pre_y = 0.0f;
+    return LBM_OK;
+}
+
+int lbm_touch_move(lbm_handle* h, float px, float py) {
+    LBM_TRY(check_handle(h));
+    if (px <= 0.0f || py <= 0.0f) {
+        h->pre_x = h->pre_y = 0.0f;
+        return LBM_IGNORED;
+    }
+    const float dx = px - h->pre_x, dy = py - h->pre_y;
+    const float dis = std::sqrt(dx * dx + dy * dy);
+    if ((h->pre_x == 0.0f && h->pre_y == 0.0f) || dis > 300.0f) {
+        h->pre_x = px;
+        h->pre_y = py;
+        return LBM_IGNORED;
+    }
+    const int r = lbm_add_external_force(h, px, py, h->pre_x, h->pre_y);
+    h->pre_x = px;
+    h->pre_y = py;
+    return r;
+}
+
+int lbm_add_external_force(lbm_handle* h, float pos_x, float pos_y, float pre_x, float pre_y) {
+    LBM_TRY(check_handle(h));
+    if (h->p.pixel_size < 2)
+        return fail(LBM_ERR_ARG, "force strokes need pixel_size >= 2 (the reference divides by pixel_size - 1)");
+    LBM_TRY(use_device(h));
+    std::vector<size_t> cells;
+    const lbm_lattice_info rec = force_stroke(h->nx, h->ny, h->p.pixel_size, pos_x, pos_y, pre_x, pre_y, cells);
+    // queue.write_buffer of one record per cell; the host copy is not updated, as in the reference
+    for (size_t k = 0; k < cells.size(); ++k) {
+        if (k > 0 && cells[k] == cells[k - 1]) continue;
+        LBM_CK(cudaMemcpyAsync(h->d_info + cells[k], &rec, sizeof(rec), cudaMemcpyHostToDevice, h->stream));
+    }
+    LBM_TRY(rebuild_flags(h));
+    return sync(h);
+}
+
+int lbm_build_mask(const lbm_params* p, lbm_lattice_info* out) {
+    if (!p || !out) return fail(LBM_ERR_ARG, "null argument");
+    LBM_TRY(validate_params(*p));
+    std::vector<lbm_lattice_info> m;
+    build_scene_mask(*p, m);
+    std::memcpy(out, m.data(), m.size() * sizeof(lbm_lattice_info));
+    return LBM_OK;
+}
+
+int lbm_mask_add_obstacle(int32_t nx, int32_t ny, lbm_lattice_info* info, int32_t x, int32_t y) {
+    if (!info) return fail(LBM_ERR_ARG, "null info");
+    const int r = (int)OBSTACLE_RADIUS;
+    if (nx < 1 || x < 0 || x >= nx || y - r < 0 || y + r > ny)
+        return fail(LBM_ERR_ARG, "obstacle rows [%d, %d) or column %d outside the lattice", y - r, y + r, x);
+    obstacle_disc(nx, x, y, info);
+    return LBM_OK;
+}
+
+int lbm_mask_force_stroke(int32_t nx, int32_t ny, int32_t pixel_size, lbm_lattice_info* info, float pos_x, float pos_y,
+                          float pre_x, float pre_y) {
+    if (!info) return fail(LBM_ERR_ARG, "null info");
+    if (pixel_size < 2) return fail(LBM_ERR_ARG, "force strokes need pixel_size >= 2");
+    std::vector<size_t> cells;
+    const lbm_lattice_info rec = force_stroke(nx, ny, pixel_size, pos_x, pos_y, pre_x, pre_y, cells);
+    for (size_t c : cells) info[c] = rec;
+    return (int)cells.size();
+}
+
+int lbm_set_info(lbm_handle* h, const lbm_lattice_info* info) {
+    LBM_TRY(check_handle(h));
+    if (!info) return fail(LBM_ERR_ARG, "null info");
+    LBM_TRY(use_device(h));
+    h->host_info.assign(info, info + h->N);
+    LBM_TRY(upload_info_rows(h, 0, h->ny));
+    LBM_TRY(rebuild_flags(h));
+    return sync(h);
+}
+
+int lbm_get_info(lbm_handle* h, lbm_lattice_info* out) {
+    LBM_TRY(check_handle(h));
+    if (!out) return fail(LBM_ERR_ARG, "null output");
+    LBM_TRY(use_device(h));
+    LBM_CK(cudaMemcpyAsync(out, h->d_info, h->N * sizeof(lbm_lattice_info), cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+int lbm_read_macro(lbm_handle* h, float* rho, float* ux, float* uy) {
+    LBM_TRY(check_handle(h));
+    LBM_TRY(use_device(h));
+    float* dst[3] = {rho, ux, uy};
+    for (int k = 0; k < 3; ++k)
+        if (dst[k])
+            LBM_CK(cudaMemcpyAsync(dst[k], h->d_macro + k * h->N, h->N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+int lbm_read_macro_rgba16f(lbm_handle* h, uint16_t* rgba) {
+    LBM_TRY(check_handle(h));
+    if (!rgba) return fail(LBM_ERR_ARG, "null output");
+    LBM_TRY(use_device(h));
+    uint16_t* d = nullptr;
+    LBM_CK(cudaMalloc((void**)&d, 4 * h->N * sizeof(uint16_t)));
+    cudaError_t e = lbm::launch_macro_rgba16f(h, d, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, d, 4 * h->N * sizeof(uint16_t), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "rgba16f read-back: %s", cudaGetErrorString(e));
+    ++h->launches;
+    return LBM_OK;
+}
+
+int lbm_read_populations(lbm_handle* h, void* dst, int32_t dd) {
+    LBM_TRY(check_handle(h));
+    if (!dst) return fail(LBM_ERR_ARG, "null output");
+    if (dd != LBM_DTYPE_F32 && dd != LBM_DTYPE_F64) return fail(LBM_ERR_ARG, "read dtype must be F32 or F64");
+    LBM_TRY(use_device(h));
+    const size_t bytes = 9 * h->N * lbm::dtype_size(dd);
+    if (h->p.mode == LBM_MODE_REFERENCE && dd == LBM_DTYPE_F32) {
+        LBM_CK(cudaMemcpyAsync(dst, h->buf[h->cur], bytes, cudaMemcpyDeviceToHost, h->stream));
+        return sync(h);
+    }
+    void* tmp = nullptr;
+    LBM_CK(cudaMalloc(&tmp, bytes));
+    cudaError_t e = lbm::launch_to_absolute(h, h->buf[h->cur], tmp, dd, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "population read-back: %s", cudaGetErrorString(e));
+    ++h->launches;
+    return LBM_OK;
+}
+
+int lbm_write_populations(lbm_handle* h, const void* src, int32_t sd) {
+    LBM_TRY(check_handle(h));
+    if (!src) return fail(LBM_ERR_ARG, "null input");
+    if (sd != LBM_DTYPE_F32 && sd != LBM_DTYPE_F64) return fail(LBM_ERR_ARG, "write dtype must be F32 or F64");
+    LBM_TRY(use_device(h));
+    const size_t bytes = 9 * h->N * lbm::dtype_size(sd);
+    void* tmp = nullptr;
+    LBM_CK(cudaMalloc(&tmp, bytes));
+    cudaError_t e = cudaMemcpyAsync(tmp, src, bytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = lbm::launch_from_absolute(h, tmp, sd, h->buf[h->cur], h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "population upload: %s", cudaGetErrorString(e));
+    ++h->launches;
+    return LBM_OK;
+}
+
+int lbm_init_equilibrium(lbm_handle* h, const float* rho, const float* ux, const float* uy) {
+    LBM_TRY(check_handle(h));
+    if (h->p.mode != LBM_MODE_PHYSICS) return fail(LBM_ERR_STATE, "equilibrium initialisation is a physics-mode call");
+    LBM_TRY(use_device(h));
+    float* d = nullptr;
+    const size_t plane = h->N * sizeof(float);
+    LBM_CK(cudaMalloc((void**)&d, 3 * plane));
+    const float* src[3] = {rho, ux, uy};
+    const float* dp[3] = {nullptr, nullptr, nullptr};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        if (src[k]) {
+            e = cudaMemcpyAsync(d + k * h->N, src[k], plane, cudaMemcpyHostToDevice, h->stream);
+            dp[k] = d + k * h->N;
+        }
+    if (e == cudaSuccess) e = lbm::launch_phys_init(h, dp[0], dp[1], dp[2], h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "equilibrium initialisation: %s", cudaGetErrorString(e));
+    ++h->launches;
+    h->cur = 0;
+    h->stepped_since_init = false;
+    return LBM_OK;
+}
+
+int lbm_conservation(lbm_handle* h, double out[3]) {
+    LBM_TRY(check_handle(h));
+    if (!out) return fail(LBM_ERR_ARG, "null output");
+    LBM_TRY(use_device(h));
+    double* d_out = h->d_part + (size_t)lbm::RED_BLOCKS * 6;
+    LBM_CK(lbm::launch_conservation(h, d_out, h->stream));
+    h->launches += 2;
+    LBM_CK(cudaMemcpyAsync(out, d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+int lbm_check_finite(lbm_handle* h, uint64_t* count) {
+    LBM_TRY(check_handle(h));
+    LBM_TRY(use_device(h));
+    LBM_CK(lbm::launch_count_nonfinite(h, h->stream));
+    ++h->launches;
+    unsigned long long n = 0;
+    LBM_CK(cudaMemcpyAsync(&n, h->d_count, sizeof(n), cudaMemcpyDeviceToHost, h->stream));
+    LBM_TRY(sync(h));
+    if (count) *count = n;
+    if (n) return fail(LBM_ERR_NAN, "%llu non-finite populations", n);
+    return LBM_OK;
+}
+
+int lbm_macro_error(lbm_handle* h, lbm_handle* ref, double out[4]) {
+    LBM_TRY(check_handle(h));
+    LBM_TRY(check_handle(ref));
+    if (!out) return fail(LBM_ERR_ARG, "null output");
+    if (h->nx != ref->nx || h->ny != ref->ny) return fail(LBM_ERR_ARG, "lattice sizes differ");
+    if (h->device != ref->device) return fail(LBM_ERR_ARG, "handles live on different devices");
+    LBM_TRY(use_device(h));
+    LBM_CK(cudaStreamSynchronize(ref->stream));
+    double* d_out = h->d_part + (size_t)lbm::RED_BLOCKS * 6 + 8;
+    LBM_CK(lbm::launch_macro_error(h, ref, d_out, h->stream));
+    h->launches += 2;
+    LBM_CK(cudaMemcpyAsync(out, d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+// ---------------------------------------------------------------------------------
+// checkpoints
+// ---------------------------------------------------------------------------------
+struct ckpt_header {
+    char magic[8];
+    uint32_t version;
+    int32_t nx, ny, mode, dtype, scene, fluid_ty, cur;
+    float tau, pre_x, pre_y;
+    int32_t stepped;
+    uint64_t steps;
+};
+
+int lbm_save(lbm_handle* h, const char* path) {
+    LBM_TRY(check_handle(h));
+    if (!path) return fail(LBM_ERR_ARG, "null path");
+    LBM_TRY(use_device(h));
+    LBM_TRY(sync(h));
+    const size_t pop_bytes = 9 * h->N * lbm::dtype_size(h->p.dtype);
+    std::vector<char> state(2 * pop_bytes);
+    std::vector<lbm_lattice_info> info(h->N);
+    std::vector<float> macro(3 * h->N);
+    LBM_CK(cudaMemcpy(state.data(), h->buf[0], pop_bytes, cudaMemcpyDeviceToHost));
+    LBM_CK(cudaMemcpy(state.data() + pop_bytes, h->buf[1], pop_bytes, cudaMemcpyDeviceToHost));
+    LBM_CK(cudaMemcpy(info.data(), h->d_info, h->N * sizeof(lbm_lattice_info), cudaMemcpyDeviceToHost));
+    LBM_CK(cudaMemcpy(macro.data(), h->d_macro, 3 * h->N * sizeof(float), cudaMemcpyDeviceToHost));
+    ckpt_header hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, "LBMCKPT1", 8);
+    hd.version = 1;
+    hd.nx = h->nx; hd.ny = h->ny; hd.mode = h->p.mode; hd.dtype = h->p.dtype; hd.scene = h->p.scene;
+    hd.fluid_ty = h->fluid_ty; hd.cur = h->cur; hd.tau = h->tau; hd.pre_x = h->pre_x; hd.pre_y = h->pre_y;
+    hd.stepped = h->stepped_since_init ? 1 : 0;
+    hd.steps = h->steps;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(LBM_ERR_IO, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
+    ok = ok && std::fwrite(state.data(), 1, state.size(), f) == state.size();
+    ok = ok && std::fwrite(info.data(), sizeof(lbm_lattice_info), h->N, f) == h->N;
+    ok = ok && std::fwrite(h->host_info.data(), sizeof(lbm_lattice_info), h->N, f) == h->N;
+    ok = ok && std::fwrite(macro.data(), sizeof(float), 3 * h->N, f) == 3 * h->N;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(LBM_ERR_IO, "short write to %s", path);
+    return LBM_OK;
+}
+
+int lbm_load(lbm_handle* h, const char* path) {
+    LBM_TRY(check_handle(h));
+    if (!path) return fail(LBM_ERR_ARG, "null path");
+    LBM_TRY(use_device(h));
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(LBM_ERR_IO, "cannot open %s", path);
+    ckpt_header hd;
+    if (std::fread(&hd, sizeof(hd), 1, f) != 1 || std::memcmp(hd.magic, "LBMCKPT1", 8) != 0 || hd.version != 1) {
+        std::fclose(f);
+        return fail(LBM_ERR_IO, "%s is not a checkpoint of this library", path);
+    }
+    if (hd.nx != h->nx || hd.ny != h->ny || hd.mode != h->p.mode || hd.dtype != h->p.dtype) {
+        std::fclose(f);
+        return fail(LBM_ERR_ARG, "checkpoint %dx%d mode %d dtype %d does not match the handle", hd.nx, hd.ny, hd.mode, hd.dtype);
+    }
+    const size_t pop_bytes = 9 * h->N * lbm::dtype_size(h->p.dtype);
+    std::vector<char> state(2 * pop_bytes);
+    std::vector<lbm_lattice_info> info(h->N), hinfo(h->N);
+    std::vector<float> macro(3 * h->N);
+    bool ok = std::fread(state.data(), 1, state.size(), f) == state.size();
+    ok = ok && std::fread(info.data(), sizeof(lbm_lattice_info), h->N, f) == h->N;
+    ok = ok && std::fread(hinfo.data(), sizeof(lbm_lattice_info), h->N, f) == h->N;
+    ok = ok && std::fread(macro.data(), sizeof(float), 3 * h->N, f) == 3 * h->N;
+    std::fclose(f);
+    if (!ok) return fail(LBM_ERR_IO, "truncated checkpoint %s", path);
+    LBM_TRY(sync(h));
+    LBM_CK(cudaMemcpy(h->buf[0], state.data(), pop_bytes, cudaMemcpyHostToDevice));
+    LBM_CK(cudaMemcpy(h->buf[1], state.data() + pop_bytes, pop_bytes, cudaMemcpyHostToDevice));
+    LBM_CK(cudaMemcpy(h->d_info, info.data(), h->N * sizeof(lbm_lattice_info), cudaMemcpyHostToDevice));
+    LBM_CK(cudaMemcpy(h->d_macro, macro.data(), 3 * h->N * sizeof(float), cudaMemcpyHostToDevice));
+    h->host_info = hinfo;
+    h->cur = hd.cur & 1;
+    h->tau = hd.tau;
+    h->omega = 1.0f / hd.tau;
+    h->pre_x = hd.pre_x;
+    h->pre_y = hd.pre_y;
+    h->stepped_since_init = hd.stepped != 0;
+    h->steps = hd.steps;
+    h->p.scene = hd.scene;
+    h->fluid_ty = hd.fluid_ty;
+    LBM_TRY(rebuild_flags(h));
+    return sync(h);
+}
+
+int lbm_steps_done(const lbm_handle* h, uint64_t* steps) {
+    LBM_TRY(check_handle(h));
+    if (steps) *steps = h->steps;
+    return LBM_OK;
+}
+
+int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches) {
+    LBM_TRY(check_handle(h));
+    if (launches) *launches = h->launches;
+    return LBM_OK;
+}
+
+int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy) {
+    LBM_TRY(check_handle(h));
+    if (rho) *rho = h->d_macro;
+    if (ux) *ux = h->d_macro + h->N;
+    if (uy) *uy = h->d_macro + 2 * h->N;
+    return LBM_OK;
+}
+
+}  // extern "C"

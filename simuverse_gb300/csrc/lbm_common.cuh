@@ -1,0 +1,92 @@
+// lbm_common.cuh -- D2Q9 constants, per-cell flag layout and population storage formats
+// shared by the step kernels.
+//
+// Lattice (simuverse/src/fluid/mod.rs:22-52): direction j has vector (EX(j), EY(j)) with y
+// growing downwards, inverse INV(j).  Reference-mode weights and clamp maxima are the
+// truncated literals of mod.rs:40-48; physics mode uses the exact 4/9, 1/9, 1/36.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lbm.h"
+
+namespace lbm {
+
+__host__ __device__ constexpr int EX(int j) {
+    return (j == 1 || j == 5 || j == 8) ? 1 : ((j == 3 || j == 6 || j == 7) ? -1 : 0);
+}
+__host__ __device__ constexpr int EY(int j) {
+    return (j == 4 || j == 7 || j == 8) ? 1 : ((j == 2 || j == 5 || j == 6) ? -1 : 0);
+}
+__host__ __device__ constexpr int INV(int j) {
+    return j == 0 ? 0 : j == 1 ? 3 : j == 2 ? 4 : j == 3 ? 1 : j == 4 ? 2 : j == 5 ? 7 : j == 6 ? 8 : j == 7 ? 5 : 6;
+}
+// mod.rs:40-48 (truncated literals, reference mode)
+__host__ __device__ constexpr float REF_W(int j) { return j == 0 ? 0.444444f : (j <= 4 ? 0.111111f : 0.0277777f); }
+__host__ __device__ constexpr float REF_MAX(int j) { return j == 0 ? 0.6f : (j <= 4 ? 0.2222f : 0.1111f); }
+// exact weights (physics mode)
+template <class R>
+__host__ __device__ constexpr R PW(int j) {
+    return j == 0 ? R(4) / R(9) : (j <= 4 ? R(1) / R(9) : R(1) / R(36));
+}
+
+// Per-cell flags (uint16), rebuilt from the info records whenever the mask changes:
+//   bits 0-3  material code (0 = unknown code, treated as plain fluid)
+//   bits 4-12 one bit per direction k = 0..8:
+//     reference mode, fluid cell: the post-collision population k is handed to the wall
+//       cell c+e_k (boundary.wgsl:28-31 moved into the owning fluid cell);
+//     reference mode, solid cell: slot k is zeroed (wall-to-wall slot, see lbm_kernels.cu);
+//     physics mode, fluid cell: the pull source of direction k is solid (bounce-back).
+//   bit 13    physics mode: some bounce-back source is a moving wall
+constexpr unsigned FL_MAT_MASK = 15u;
+constexpr int FL_DIR_SHIFT = 4;
+constexpr unsigned FL_MOVING = 1u << 13;
+
+__host__ __device__ constexpr bool is_solid(int m) { return m == LBM_BOUNDARY || m == LBM_OBSTACLE; }
+
+// ---- population storage formats ------------------------------------------------
+// R: arithmetic type; T: stored type.  Physics-mode storage holds d = f - w (shifted
+// deviation); FP16 additionally scales by 2^10 so that small deviations stay normal.
+struct StoreF32 {
+    using T = float;
+    using R = float;
+    static constexpr int dtype = LBM_DTYPE_F32;
+    __device__ __forceinline__ static R ld(const T* p) { return __ldg(p); }
+    __device__ __forceinline__ static void st(T* p, R v) { *p = v; }
+    __host__ __device__ static R to_r(T v) { return v; }
+    __host__ __device__ static T from_r(R v) { return v; }
+};
+struct StoreF64 {
+    using T = double;
+    using R = double;
+    static constexpr int dtype = LBM_DTYPE_F64;
+    __device__ __forceinline__ static R ld(const T* p) { return __ldg(p); }
+    __device__ __forceinline__ static void st(T* p, R v) { *p = v; }
+    __host__ __device__ static R to_r(T v) { return v; }
+    __host__ __device__ static T from_r(R v) { return v; }
+};
+constexpr float F16_SCALE = 1024.0f;
+constexpr float F16_INV_SCALE = 1.0f / 1024.0f;
+struct StoreF16 {
+    using T = __half;
+    using R = float;
+    static constexpr int dtype = LBM_DTYPE_F16;
+    __device__ __forceinline__ static R ld(const T* p) { return __half2float(__ldg(p)) * F16_INV_SCALE; }
+    __device__ __forceinline__ static void st(T* p, R v) { *p = __float2half_rn(v * F16_SCALE); }
+    __host__ __device__ static R to_r(T v) { return __half2float(v) * F16_INV_SCALE; }
+    __host__ __device__ static T from_r(R v) { return __float2half_rn(v * F16_SCALE); }
+};
+struct StoreBF16 {
+    using T = __nv_bfloat16;
+    using R = float;
+    static constexpr int dtype = LBM_DTYPE_BF16;
+    __device__ __forceinline__ static R ld(const T* p) { return __bfloat162float(__ldg(p)); }
+    __device__ __forceinline__ static void st(T* p, R v) { *p = __float2bfloat16_rn(v); }
+    __host__ __device__ static R to_r(T v) { return __bfloat162float(v); }
+    __host__ __device__ static T from_r(R v) { return __float2bfloat16_rn(v); }
+};
+
+}  // namespace lbm

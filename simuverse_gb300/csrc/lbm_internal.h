@@ -1,0 +1,58 @@
+// lbm_internal.h -- handle layout and kernel launchers shared by the C ABI (lbm_api.cpp)
+// and the kernels (lbm_kernels.cu).  Not installed; the public surface is include/lbm.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lbm.h"
+
+struct lbm_handle {
+    lbm_params p;
+    int nx = 0, ny = 0;
+    size_t N = 0;
+    int fluid_ty = 0;  // d2q9_node.rs:53-57: 1 for the cavity, else 0
+    float tau = 0.6f, omega = 1.0f / 0.6f;
+    void* buf[2] = {nullptr, nullptr};  // ping-pong population buffers (9*N each)
+    int cur = 0;                        // buffer holding the state the next step reads
+    uint16_t* d_flags = nullptr;
+    lbm_lattice_info* d_info = nullptr;
+    std::vector<lbm_lattice_info> host_info;  // D2Q9Node::lattice_info_data
+    float* d_macro = nullptr;                 // rho, ux, uy planes
+    double* d_part = nullptr;                 // reduction partials
+    unsigned long long* d_count = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    uint64_t steps = 0;
+    uint64_t launches = 0;
+    bool stepped_since_init = false;  // macro_tex holds (0,0,0,1) right after init
+    float pre_x = 0.0f, pre_y = 0.0f;  // FluidSimulator::pre_pos
+    int device = 0;
+};
+
+namespace lbm {
+
+constexpr int TPB = 128;          // threads per block along x for the step kernels
+constexpr int RED_BLOCKS = 1216;  // 8 x 152 SMs; fixed so FP64 sums have a fixed order
+constexpr int RED_TPB = 256;
+
+inline size_t dtype_size(int dtype) { return dtype == LBM_DTYPE_F64 ? 8 : (dtype == LBM_DTYPE_F32 ? 4 : 2); }
+
+// Kernel launchers (lbm_kernels.cu).  All return cudaGetLastError() of the launch.
+cudaError_t launch_build_flags(const lbm_handle* h, cudaStream_t s);
+cudaError_t launch_ref_init(lbm_handle* h, cudaStream_t s);
+cudaError_t launch_phys_init(lbm_handle* h, const float* d_rho, const float* d_ux, const float* d_uy,
+                             cudaStream_t s);
+cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s);
+cudaError_t launch_conservation(lbm_handle* h, double* d_out3, cudaStream_t s);
+cudaError_t launch_count_nonfinite(lbm_handle* h, cudaStream_t s);
+cudaError_t launch_macro_error(lbm_handle* h, lbm_handle* ref, double* d_out4, cudaStream_t s);
+cudaError_t launch_macro_rgba16f(lbm_handle* h, uint16_t* d_rgba, cudaStream_t s);
+cudaError_t launch_to_absolute(lbm_handle* h, const void* state, void* dst, int dst_dtype, cudaStream_t s);
+cudaError_t launch_from_absolute(lbm_handle* h, const void* src, int src_dtype, void* state, cudaStream_t s);
+
+}  // namespace lbm

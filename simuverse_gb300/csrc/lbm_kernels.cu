@@ -1,0 +1,643 @@
+// lbm_kernels.cu -- sm_103a kernels of the D2Q9 step and its helpers.
+//
+// One fused pass per time step replaces the reference's two dispatches
+// (collide_stream.wgsl then boundary.wgsl, d2q9_node.rs:302-312):
+//   * pull streaming from the ping-pong buffer A (layout_and_fn.wgsl:38-51),
+//   * moments, forcing and BGK collision (collide_stream.wgsl:43-87),
+//   * the bounce-back of boundary.wgsl:3-35, folded into the owning fluid cell: a fluid
+//     cell strictly inside the outer ring whose neighbour c+e_i is solid writes its
+//     post-collision population i into the wall slot (c+e_i, inv(i)) and a zero into its
+//     own slot (c, i), which is exactly what the boundary dispatch leaves behind.  Each wall
+//     slot has one writer, so the pass is race-free.  Wall-to-wall slots (both cells solid)
+//     are never read by a fluid cell; the reference's boundary dispatch races on them, and
+//     this kernel sets them to zero, one of the outcomes that race can produce.
+//   * the macro field (rho, ux, uy) when requested (collide_stream.wgsl:36,74).
+//
+// Reference mode reproduces the WGSL arithmetic operation by operation with explicit
+// round-to-nearest intrinsics (no multiply-add contraction), so it agrees bit for bit with
+// a CPU restatement compiled with contraction off.  Physics mode is a standard BGK step
+// with exact weights, stored as deviations f - w.
+#include "lbm_common.cuh"
+#include "lbm_internal.h"
+
+namespace lbm {
+
+// ------------------------------------------------------------------------------------
+// flags
+// ------------------------------------------------------------------------------------
+__global__ void k_build_flags(const lbm_lattice_info* __restrict__ info, uint16_t* __restrict__ flags, int nx,
+                              int ny, int mode) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= nx) return;
+    const size_t c = (size_t)y * nx + x;
+    const int code = info[c].material;
+    unsigned fl = (code >= 0 && code <= 15) ? (unsigned)code : 0u;
+    auto inside = [&](int xx, int yy) { return xx > 0 && yy > 0 && xx < nx - 1 && yy < ny - 1; };
+    if (mode == LBM_MODE_REFERENCE) {
+        if (is_solid(code)) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const int px = x + EX(k), py = y + EY(k);
+                if (px < 0 || py < 0 || px >= nx || py >= ny) continue;
+                if (is_solid(info[(size_t)py * nx + px].material) && (inside(x, y) || inside(px, py)))
+                    fl |= 1u << (FL_DIR_SHIFT + k);
+            }
+        } else if (inside(x, y)) {
+#pragma unroll
+            for (int k = 1; k < 9; ++k) {
+                if (is_solid(info[(size_t)(y + EY(k)) * nx + (x + EX(k))].material)) fl |= 1u << (FL_DIR_SHIFT + k);
+            }
+        }
+    } else {
+        if (!is_solid(code)) {
+#pragma unroll
+            for (int j = 1; j < 9; ++j) {
+                int sx = x - EX(j), sy = y - EY(j);
+                if (code == LBM_OUTLET && EX(j) == -1) sx = x;
+                sx = sx < 0 ? nx - 1 : (sx >= nx ? 0 : sx);
+                sy = sy < 0 ? ny - 1 : (sy >= ny ? 0 : sy);
+                const lbm_lattice_info s = info[(size_t)sy * nx + sx];
+                if (is_solid(s.material)) {
+                    fl |= 1u << (FL_DIR_SHIFT + j);
+                    if (s.vx != 0.0f || s.vy != 0.0f) fl |= FL_MOVING;
+                }
+            }
+        }
+    }
+    flags[c] = (uint16_t)fl;
+}
+
+// ------------------------------------------------------------------------------------
+// initialisation
+// ------------------------------------------------------------------------------------
+// init.wgsl:19-63
+__global__ void k_ref_init(float* __restrict__ A, float* __restrict__ B, lbm_lattice_info* __restrict__ info,
+                           uint16_t* __restrict__ flags, int nx, int ny, int fluid_ty, float* __restrict__ macro) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= nx) return;
+    const size_t N = (size_t)nx * ny;
+    const size_t c = (size_t)y * nx + x;
+    lbm_lattice_info in = info[c];
+    if (is_solid(in.material)) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { A[c + i * N] = 0.0f; B[c + i * N] = 0.0f; }
+    } else if (fluid_ty == 0) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { A[c + i * N] = REF_W(i); B[c + i * N] = 0.0f; }
+        const float temp = __fmul_rn(REF_W(3), 0.5f);
+        A[c + 1 * N] = __fadd_rn(REF_W(1), temp);
+        A[c + 3 * N] = temp;
+        B[c + 1 * N] = __fadd_rn(REF_W(1), temp);
+        B[c + 3 * N] = temp;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { A[c + i * N] = REF_W(i); B[c + i * N] = 0.0f; }
+    }
+    if ((in.material == LBM_INLET || in.material == LBM_EXTERNAL_FORCE) && in.block_iter > 0) {
+        in.block_iter = 0;
+        in.material = LBM_BULK;
+        in.vx = 0.0f;
+        in.vy = 0.0f;
+        info[c] = in;
+        flags[c] = (uint16_t)((flags[c] & ~FL_MAT_MASK) | LBM_BULK);
+    }
+    macro[c] = 0.0f;
+    macro[c + N] = 0.0f;
+    macro[c + 2 * N] = 0.0f;
+}
+
+template <class ST>
+__global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
+                            const lbm_lattice_info* __restrict__ info, const float* __restrict__ rho_in,
+                            const float* __restrict__ ux_in, const float* __restrict__ uy_in, int nx, int ny,
+                            float* __restrict__ macro) {
+    using R = typename ST::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= nx) return;
+    const size_t N = (size_t)nx * ny;
+    const size_t c = (size_t)y * nx + x;
+    if (is_solid(info[c].material)) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { ST::st(A + c + i * N, R(0)); ST::st(B + c + i * N, R(0)); }
+        macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f;
+        return;
+    }
+    const R rho = rho_in ? R(rho_in[c]) : R(1);
+    const R ux = ux_in ? R(ux_in[c]) : R(0);
+    const R uy = uy_in ? R(uy_in[c]) : R(0);
+    const R drho = rho - R(1);
+    const R usq = R(1.5) * (ux * ux + uy * uy);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const R eu = R(EX(i)) * ux + R(EY(i)) * uy;
+        const R d = PW<R>(i) * (drho + rho * (R(3) * eu + R(4.5) * (eu * eu) - usq));
+        ST::st(A + c + i * N, d);
+        ST::st(B + c + i * N, d);
+    }
+    macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy;
+}
+
+// ------------------------------------------------------------------------------------
+// reference-mode step: collide_stream.wgsl:25-88 + boundary.wgsl:3-35, one pass
+// ------------------------------------------------------------------------------------
+template <bool MACRO>
+__global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, float* __restrict__ B,
+                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
+                                                  float omega, int nx, int ny, float* __restrict__ macro) {
+    const int x = blockIdx.x * TPB + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= nx) return;
+    const size_t N = (size_t)nx * ny;
+    const size_t c = (size_t)y * nx + x;
+    const unsigned fl = flags[c];
+    const int m = (int)(fl & FL_MAT_MASK);
+    if (is_solid(m)) {  // collide_stream.wgsl:34-38
+        if (MACRO) { macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f; }
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            if (fl & (1u << (FL_DIR_SHIFT + k))) B[c + k * N] = 0.0f;
+        return;
+    }
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
+    float f[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {  // source uv - e(j), wrapped
+        const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? xp : x);
+        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+        f[j] = __ldg(A + row + sx + (size_t)j * N);
+    }
+    float rho = 0.0f, vx = 0.0f, vy = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        rho = __fadd_rn(rho, f[j]);
+        vx = __fadd_rn(vx, __fmul_rn((float)EX(j), f[j]));
+        vy = __fadd_rn(vy, __fmul_rn((float)EY(j), f[j]));
+    }
+    rho = fminf(fmaxf(rho, 0.8f), 1.2f);
+    vx = __fdiv_rn(vx, rho);
+    vy = __fdiv_rn(vy, rho);
+    float F[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) F[j] = 0.0f;
+    if (m == LBM_INLET || m == LBM_EXTERNAL_FORCE) {  // collide_stream.wgsl:55-71
+        lbm_lattice_info in = info[c];
+        if (in.block_iter > 0) {
+            in.block_iter = in.block_iter - 1;
+            if (in.block_iter == 0) {
+                in.material = LBM_BULK;
+                flags[c] = (uint16_t)((fl & ~FL_MAT_MASK) | LBM_BULK);
+            }
+            info[c] = in;
+        }
+        const float fx = in.vx, fy = in.vy;
+        vx = __fdiv_rn(__fmul_rn(fx, 0.5f), rho);
+        vy = __fdiv_rn(__fmul_rn(fy, 0.5f), rho);
+#pragma unroll
+        for (int j = 0; j < 9; ++j)
+            F[j] = __fmul_rn(__fmul_rn(REF_W(j), 3.0f),
+                             __fadd_rn(__fmul_rn((float)EX(j), fx), __fmul_rn((float)EY(j), fy)));
+    }
+    if (MACRO) { macro[c] = rho; macro[c + N] = vx; macro[c + 2 * N] = vy; }
+    const float usqr = __fmul_rn(1.5f, __fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)));
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const float eu = __fadd_rn(__fmul_rn((float)EX(j), vx), __fmul_rn((float)EY(j), vy));
+        const float feq = __fmul_rn(__fmul_rn(rho, REF_W(j)),
+                                    __fsub_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(3.0f, eu)), __fmul_rn(4.5f, __fmul_rn(eu, eu))),
+                                              usqr));
+        float t = __fadd_rn(__fsub_rn(f[j], __fmul_rn(omega, __fsub_rn(f[j], feq))), F[j]);
+        if (t > REF_MAX(j)) t = REF_MAX(j);
+        else if (t < 0.0f) t = 0.0f;
+        if (fl & (1u << (FL_DIR_SHIFT + j))) {
+            B[c + (size_t)EY(j) * nx + EX(j) + (size_t)INV(j) * N] = t;
+            B[c + (size_t)j * N] = 0.0f;
+        } else {
+            B[c + (size_t)j * N] = t;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// physics-mode step
+// ------------------------------------------------------------------------------------
+template <class ST, bool MACRO>
+__global__ void __launch_bounds__(TPB) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
+                                                   uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
+                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro) {
+    using R = typename ST::R;
+    const int x = blockIdx.x * TPB + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= nx) return;
+    const size_t N = (size_t)nx * ny;
+    const size_t c = (size_t)y * nx + x;
+    const unsigned fl = flags[c];
+    const int m = (int)(fl & FL_MAT_MASK);
+    if (is_solid(m)) {
+        if (MACRO) { macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f; }
+        return;
+    }
+    const bool outlet = (m == LBM_OUTLET);
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
+    R d[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
+        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+        if (fl & (1u << (FL_DIR_SHIFT + j))) {
+            R v = ST::ld(A + c + (size_t)INV(j) * N);  // half-way bounce-back
+            if (fl & FL_MOVING) {
+                const lbm_lattice_info si = info[row + sx];
+                const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
+                if (uw != R(0)) v = v + R(6) * PW<R>(j) * uw;
+            }
+            d[j] = v;
+        } else {
+            d[j] = ST::ld(A + row + sx + (size_t)j * N);
+        }
+    }
+    if (m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
+        const lbm_lattice_info in = info[c];
+        const R ux = R(in.vx), uy = R(in.vy);
+        const R S = d[0] + d[2] + d[4] + R(2) * (d[3] + d[6] + d[7]);
+        const R rho = (R(1) + S) / (R(1) - ux);
+        const R rux = rho * ux, ruy = rho * uy;
+        d[1] = d[3] + (R(2) / R(3)) * rux;
+        d[5] = d[7] + R(0.5) * (d[4] - d[2]) + rux / R(6) - R(0.5) * ruy;
+        d[8] = d[6] + R(0.5) * (d[2] - d[4]) + rux / R(6) + R(0.5) * ruy;
+    }
+    if (outlet) {  // zero-gradient outflow anchored at rho = 1: f_j <- f_j / rho
+        const R dr = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
+        const R inv = R(1) / (R(1) + dr);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) d[j] = (d[j] - PW<R>(j) * dr) * inv;
+    }
+    const R drho = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
+    R jx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
+    R jy = (d[4] - d[2]) + (d[7] - d[5]) + (d[8] - d[6]);
+    const R rho = R(1) + drho;
+    R Fx = R(0), Fy = R(0);
+    const bool forced = (m == LBM_EXTERNAL_FORCE);
+    if (forced) {  // Guo forcing with the reference's block_iter countdown
+        lbm_lattice_info in = info[c];
+        if (in.block_iter > 0) {
+            in.block_iter = in.block_iter - 1;
+            if (in.block_iter == 0) {
+                in.material = LBM_BULK;
+                flags[c] = (uint16_t)((fl & ~FL_MAT_MASK) | LBM_BULK);
+            }
+            info[c] = in;
+        }
+        Fx = R(in.vx);
+        Fy = R(in.vy);
+        jx = jx + R(0.5) * Fx;
+        jy = jy + R(0.5) * Fy;
+    }
+    const R ux = jx / rho, uy = jy / rho;
+    if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
+    const R usq = R(1.5) * (ux * ux + uy * uy);
+    const R gf = R(1) - R(0.5) * omega;
+    R o[9];
+#pragma unroll
+    for (int j = 1; j < 9; ++j) {
+        const R ex = R(EX(j)), ey = R(EY(j));
+        const R eu = ex * ux + ey * uy;
+        const R deq = PW<R>(j) * (drho + rho * (R(3) * eu + R(4.5) * (eu * eu) - usq));
+        R out = d[j] - omega * (d[j] - deq);
+        if (forced) {
+            const R eF = ex * Fx + ey * Fy;
+            const R uF = ux * Fx + uy * Fy;
+            out = out + gf * PW<R>(j) * (R(3) * (eF - uF) + R(9) * eu * eF);
+        }
+        o[j] = out;
+    }
+    // rest population from mass conservation: sum_j o_j = drho by construction (the BGK
+    // value in exact arithmetic; removes the bias of the rounded weights' moments)
+    o[0] = drho - (((o[1] + o[3]) + (o[2] + o[4])) + ((o[5] + o[7]) + (o[6] + o[8])));
+#pragma unroll
+    for (int j = 0; j < 9; ++j) ST::st(B + c + (size_t)j * N, o[j]);
+}
+
+// ------------------------------------------------------------------------------------
+// FP64 reductions (fixed grid, fixed order -> deterministic)
+// ------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void block_reduce_sum(double (&v)[K], double* smem /* K * 32 */) {
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) smem[k * 32 + warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            v[k] = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        }
+    }
+}
+
+template <class ST, int MODE>
+__global__ void __launch_bounds__(RED_TPB) k_conservation(const typename ST::T* __restrict__ A,
+                                                          const uint16_t* __restrict__ flags, size_t N,
+                                                          double* __restrict__ part) {
+    __shared__ double smem[3 * 32];
+    double v[3] = {0.0, 0.0, 0.0};
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += stride) {
+        const bool solid = is_solid((int)(flags[c] & FL_MAT_MASK));
+        if (MODE == LBM_MODE_PHYSICS && solid) continue;
+        if (MODE == LBM_MODE_PHYSICS) v[0] += 1.0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const double f = (double)ST::to_r(A[c + (size_t)j * N]);
+            v[0] += f;
+            v[1] += (double)EX(j) * f;
+            v[2] += (double)EY(j) * f;
+        }
+    }
+    block_reduce_sum<3>(v, smem);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x * 3 + 0] = v[0];
+        part[blockIdx.x * 3 + 1] = v[1];
+        part[blockIdx.x * 3 + 2] = v[2];
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(RED_TPB) k_final_sum(const double* __restrict__ part, int nparts,
+                                                       double* __restrict__ out) {
+    __shared__ double smem[K * 32];
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] += part[b * K + k];
+    block_reduce_sum<K>(v, smem);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = v[k];
+}
+
+template <class ST>
+__global__ void k_count_nonfinite(const typename ST::T* __restrict__ A, size_t total, unsigned long long* count) {
+    unsigned long long local = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        const double v = (double)ST::to_r(A[i]);
+        if (!isfinite(v)) ++local;
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+// sums over non-solid cells of h: |drho|^2, |rho_ref|^2, |du|^2, |u_ref|^2, then maxima
+__global__ void __launch_bounds__(RED_TPB) k_macro_error(const float* __restrict__ m, const float* __restrict__ mref,
+                                                         const uint16_t* __restrict__ flags, size_t N,
+                                                         double* __restrict__ part) {
+    __shared__ double smem[6 * 32];
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += stride) {
+        if (is_solid((int)(flags[c] & FL_MAT_MASK))) continue;
+        const double r = m[c], rr = mref[c];
+        const double ux = m[c + N], uy = m[c + 2 * N], rux = mref[c + N], ruy = mref[c + 2 * N];
+        const double dr = r - rr, dux = ux - rux, duy = uy - ruy;
+        v[0] += dr * dr;
+        v[1] += rr * rr;
+        v[2] += dux * dux + duy * duy;
+        v[3] += rux * rux + ruy * ruy;
+        v[4] = fmax(v[4], sqrt(dux * dux + duy * duy));
+        v[5] = fmax(v[5], fabs(dr));
+    }
+    // sums
+    double s[4] = {v[0], v[1], v[2], v[3]};
+    block_reduce_sum<4>(s, smem);
+    __syncthreads();
+    // maxima
+    double mx[2] = {v[4], v[5]};
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx[k] = fmax(mx[k], __shfl_down_sync(0xffffffffu, mx[k], o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { smem[warp] = mx[0]; smem[32 + warp] = mx[1]; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a = fmax(a, smem[w]); b = fmax(b, smem[32 + w]); }
+        part[blockIdx.x * 6 + 0] = s[0];
+        part[blockIdx.x * 6 + 1] = s[1];
+        part[blockIdx.x * 6 + 2] = s[2];
+        part[blockIdx.x * 6 + 3] = s[3];
+        part[blockIdx.x * 6 + 4] = a;
+        part[blockIdx.x * 6 + 5] = b;
+    }
+}
+
+__global__ void k_macro_error_final(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s[4] = {0, 0, 0, 0}, a = 0, b = 0;
+    for (int i = 0; i < nparts; ++i) {
+        for (int k = 0; k < 4; ++k) s[k] += part[i * 6 + k];
+        a = fmax(a, part[i * 6 + 4]);
+        b = fmax(b, part[i * 6 + 5]);
+    }
+    out[0] = s[1] > 0 ? sqrt(s[0] / s[1]) : sqrt(s[0]);
+    out[1] = s[3] > 0 ? sqrt(s[2] / s[3]) : sqrt(s[2]);
+    out[2] = a;
+    out[3] = b;
+}
+
+// ------------------------------------------------------------------------------------
+// conversions
+// ------------------------------------------------------------------------------------
+__global__ void k_macro_rgba16f(const float* __restrict__ macro, const uint16_t* __restrict__ flags, size_t N,
+                                int stepped, ushort4* __restrict__ out) {
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const bool solid = is_solid((int)(flags[c] & FL_MAT_MASK));
+    ushort4 o;
+    o.x = __half_as_ushort(__float2half_rn(macro[c + N]));
+    o.y = __half_as_ushort(__float2half_rn(macro[c + 2 * N]));
+    o.z = __half_as_ushort(__float2half_rn(macro[c]));
+    o.w = __half_as_ushort(__float2half_rn((stepped && solid) ? 0.0f : 1.0f));
+    out[c] = o;
+}
+
+template <class ST, class D>
+__global__ void k_to_absolute(const typename ST::T* __restrict__ s, D* __restrict__ dst, size_t N, int mode) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * N) return;
+    const int j = (int)(i / N);
+    using R = typename ST::R;
+    const R v = ST::to_r(s[i]);
+    if (mode == LBM_MODE_REFERENCE) dst[i] = (D)v;
+    else dst[i] = (D)PW<D>(j) + (D)v;
+}
+
+template <class ST, class D>
+__global__ void k_from_absolute(const D* __restrict__ src, typename ST::T* __restrict__ s, size_t N, int mode) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * N) return;
+    const int j = (int)(i / N);
+    using R = typename ST::R;
+    if (mode == LBM_MODE_REFERENCE) s[i] = ST::from_r((R)src[i]);
+    else s[i] = ST::from_r((R)(src[i] - PW<D>(j)));
+}
+
+// ------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------
+static inline dim3 cell_grid(const lbm_handle* h) { return dim3((unsigned)((h->nx + TPB - 1) / TPB), (unsigned)h->ny); }
+
+cudaError_t launch_build_flags(const lbm_handle* h, cudaStream_t s) {
+    k_build_flags<<<cell_grid(h), TPB, 0, s>>>(h->d_info, h->d_flags, h->nx, h->ny, h->p.mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ref_init(lbm_handle* h, cudaStream_t s) {
+    k_ref_init<<<cell_grid(h), TPB, 0, s>>>((float*)h->buf[0], (float*)h->buf[1], h->d_info, h->d_flags, h->nx, h->ny,
+                                             h->fluid_ty, h->d_macro);
+    return cudaGetLastError();
+}
+
+template <class ST>
+static cudaError_t phys_init_t(lbm_handle* h, const float* r, const float* ux, const float* uy, cudaStream_t s) {
+    k_phys_init<ST><<<cell_grid(h), TPB, 0, s>>>((typename ST::T*)h->buf[0], (typename ST::T*)h->buf[1], h->d_info, r, ux,
+                                                 uy, h->nx, h->ny, h->d_macro);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phys_init(lbm_handle* h, const float* r, const float* ux, const float* uy, cudaStream_t s) {
+    switch (h->p.dtype) {
+        case LBM_DTYPE_F32: return phys_init_t<StoreF32>(h, r, ux, uy, s);
+        case LBM_DTYPE_F64: return phys_init_t<StoreF64>(h, r, ux, uy, s);
+        case LBM_DTYPE_F16: return phys_init_t<StoreF16>(h, r, ux, uy, s);
+        default: return phys_init_t<StoreBF16>(h, r, ux, uy, s);
+    }
+}
+
+template <class ST, bool MACRO>
+static cudaError_t phys_step_t(lbm_handle* h, cudaStream_t s) {
+    using T = typename ST::T;
+    k_phys_step<ST, MACRO><<<cell_grid(h), TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
+                                                        h->d_info, (typename ST::R)h->omega, h->nx, h->ny, h->d_macro);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
+    if (h->p.mode == LBM_MODE_REFERENCE) {
+        const float* A = (const float*)h->buf[h->cur];
+        float* B = (float*)h->buf[h->cur ^ 1];
+        if (write_macro)
+            k_ref_step<true><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+        else
+            k_ref_step<false><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+        return cudaGetLastError();
+    }
+    switch (h->p.dtype) {
+        case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
+        case LBM_DTYPE_F64: return write_macro ? phys_step_t<StoreF64, true>(h, s) : phys_step_t<StoreF64, false>(h, s);
+        case LBM_DTYPE_F16: return write_macro ? phys_step_t<StoreF16, true>(h, s) : phys_step_t<StoreF16, false>(h, s);
+        default: return write_macro ? phys_step_t<StoreBF16, true>(h, s) : phys_step_t<StoreBF16, false>(h, s);
+    }
+}
+
+template <class ST>
+static cudaError_t conservation_t(lbm_handle* h, double* out, cudaStream_t s) {
+    const auto* A = (const typename ST::T*)h->buf[h->cur];
+    if (h->p.mode == LBM_MODE_REFERENCE)
+        k_conservation<ST, LBM_MODE_REFERENCE><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, h->d_flags, h->N, h->d_part);
+    else
+        k_conservation<ST, LBM_MODE_PHYSICS><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, h->d_flags, h->N, h->d_part);
+    k_final_sum<3><<<1, RED_TPB, 0, s>>>(h->d_part, RED_BLOCKS, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conservation(lbm_handle* h, double* out, cudaStream_t s) {
+    switch (h->p.dtype) {
+        case LBM_DTYPE_F32: return conservation_t<StoreF32>(h, out, s);
+        case LBM_DTYPE_F64: return conservation_t<StoreF64>(h, out, s);
+        case LBM_DTYPE_F16: return conservation_t<StoreF16>(h, out, s);
+        default: return conservation_t<StoreBF16>(h, out, s);
+    }
+}
+
+cudaError_t launch_count_nonfinite(lbm_handle* h, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(h->d_count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    const size_t total = 9 * h->N;
+    switch (h->p.dtype) {
+        case LBM_DTYPE_F32: k_count_nonfinite<StoreF32><<<RED_BLOCKS, RED_TPB, 0, s>>>((const float*)h->buf[h->cur], total, h->d_count); break;
+        case LBM_DTYPE_F64: k_count_nonfinite<StoreF64><<<RED_BLOCKS, RED_TPB, 0, s>>>((const double*)h->buf[h->cur], total, h->d_count); break;
+        case LBM_DTYPE_F16: k_count_nonfinite<StoreF16><<<RED_BLOCKS, RED_TPB, 0, s>>>((const __half*)h->buf[h->cur], total, h->d_count); break;
+        default: k_count_nonfinite<StoreBF16><<<RED_BLOCKS, RED_TPB, 0, s>>>((const __nv_bfloat16*)h->buf[h->cur], total, h->d_count); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_macro_error(lbm_handle* h, lbm_handle* ref, double* out, cudaStream_t s) {
+    k_macro_error<<<RED_BLOCKS, RED_TPB, 0, s>>>(h->d_macro, ref->d_macro, h->d_flags, h->N, h->d_part);
+    k_macro_error_final<<<1, 32, 0, s>>>(h->d_part, RED_BLOCKS, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_macro_rgba16f(lbm_handle* h, uint16_t* d_rgba, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((h->N + 255) / 256);
+    k_macro_rgba16f<<<blocks, 256, 0, s>>>(h->d_macro, h->d_flags, h->N, h->stepped_since_init ? 1 : 0, (ushort4*)d_rgba);
+    return cudaGetLastError();
+}
+
+template <class ST>
+static cudaError_t to_abs_t(lbm_handle* h, const void* state, void* dst, int dd, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((9 * h->N + 255) / 256);
+    if (dd == LBM_DTYPE_F64)
+        k_to_absolute<ST, double><<<blocks, 256, 0, s>>>((const typename ST::T*)state, (double*)dst, h->N, h->p.mode);
+    else
+        k_to_absolute<ST, float><<<blocks, 256, 0, s>>>((const typename ST::T*)state, (float*)dst, h->N, h->p.mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_absolute(lbm_handle* h, const void* state, void* dst, int dd, cudaStream_t s) {
+    switch (h->p.dtype) {
+        case LBM_DTYPE_F32: return to_abs_t<StoreF32>(h, state, dst, dd, s);
+        case LBM_DTYPE_F64: return to_abs_t<StoreF64>(h, state, dst, dd, s);
+        case LBM_DTYPE_F16: return to_abs_t<StoreF16>(h, state, dst, dd, s);
+        default: return to_abs_t<StoreBF16>(h, state, dst, dd, s);
+    }
+}
+
+template <class ST>
+static cudaError_t from_abs_t(lbm_handle* h, const void* src, int sd, void* state, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((9 * h->N + 255) / 256);
+    if (sd == LBM_DTYPE_F64)
+        k_from_absolute<ST, double><<<blocks, 256, 0, s>>>((const double*)src, (typename ST::T*)state, h->N, h->p.mode);
+    else
+        k_from_absolute<ST, float><<<blocks, 256, 0, s>>>((const float*)src, (typename ST::T*)state, h->N, h->p.mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_absolute(lbm_handle* h, const void* src, int sd, void* state, cudaStream_t s) {
+    switch (h->p.dtype) {
+        case LBM_DTYPE_F32: return from_abs_t<StoreF32>(h, src, sd, state, s);
+        case LBM_DTYPE_F64: return from_abs_t<StoreF64>(h, src, sd, state, s);
+        case LBM_DTYPE_F16: return from_abs_t<StoreF16>(h, src, sd, state, s);
+        default: return from_abs_t<StoreBF16>(h, src, sd, state, s);
+    }
+}
+
+}  // namespace lbm

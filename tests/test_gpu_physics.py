@@ -1,0 +1,129 @@
+"""Physics-mode parity (exact weights, half-way bounce-back, moving lid, Zou-He inlet,
+zero-gradient outflow) of the CUDA step against the oracle, plus analytic checks.
+
+Tolerances: FP32 max relative error <= 1e-5 on rho and u after one step (velocity
+normalised by the lid / inlet speed) and relative L2 <= 1e-4 after 1000 steps; FP64
+<= 1e-12; FP32 mass drift <= 1e-10 relative over 1000 steps of a closed cavity.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_l2
+from simuverse_gb300 import FluidSimulator
+
+pytestmark = pytest.mark.gpu
+
+
+def _macro_err(sim, ref, u_scale):
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    e_rho = float(np.max(np.abs(rho - r_rho)))
+    e_u = float(max(np.max(np.abs(ux - r_ux)), np.max(np.abs(uy - r_uy)))) / u_scale
+    return e_rho, e_u
+
+
+def test_cavity_fp32_parity_and_mass(gpu):
+    nx = ny = 256
+    sim = FluidSimulator(nx, ny, mode="physics", scene="cavity", tau=0.6, lid_speed=0.1)
+    info = oracle.mask_physics_cavity(nx, ny, 0.1)
+    assert np.array_equal(sim.info(), info)
+    ref = oracle.PhysOracle(info, 0.6, np.float32)
+    m0 = sim.conservation()[0]
+    sim.step(1)
+    ref.step(1)
+    e_rho, e_u = _macro_err(sim, ref, 0.1)
+    assert e_rho <= 1e-5 and e_u <= 1e-5
+    sim.step(999)
+    ref.step(999)
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(rho, r_rho) <= 1e-4
+    assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= 1e-4
+    m1 = sim.conservation()[0]
+    assert abs(m1 - m0) / m0 <= 1e-10
+    mo = ref.conservation()[0]
+    assert abs(m1 - mo) / mo <= 1e-10
+
+
+def test_cavity_fp64_parity(gpu):
+    nx, ny = 96, 80
+    sim = FluidSimulator(nx, ny, mode="physics", dtype="f64", scene="cavity", tau=0.55, lid_speed=0.08)
+    ref = oracle.PhysOracle(oracle.mask_physics_cavity(nx, ny, 0.08), 0.55, np.float64)
+    sim.step(300)
+    ref.step(300)
+    e_rho, e_u = _macro_err(sim, ref, 0.08)
+    assert e_rho <= 1e-6 and e_u <= 1e-6  # macro planes are FP32
+    f = sim.read_populations(np.float64)
+    assert np.max(np.abs(f - ref.populations(np.float64))) <= 1e-12
+    m_sim, m_ref = sim.conservation()[0], ref.conservation()[0]
+    assert abs(m_sim - m_ref) / m_ref <= 1e-13
+
+
+def test_channel_fp32_parity(gpu):
+    nx, ny = 384, 160
+    kw = dict(inlet_speed=0.05, seed=11, solid_fraction=0.05, disk_radius=(5.0, 12.0))
+    sim = FluidSimulator(nx, ny, mode="physics", scene="channel", tau=0.56, **kw)
+    info, ndisk = oracle.mask_physics_channel(nx, ny, 0.05, 11, 0.05, 5.0, 12.0)
+    assert ndisk > 3
+    assert np.array_equal(sim.info(), info)
+    ref = oracle.PhysOracle(info, 0.56, np.float32)
+    sim.step(1)
+    ref.step(1)
+    e_rho, e_u = _macro_err(sim, ref, 0.05)
+    assert e_rho <= 1e-5 and e_u <= 1e-5
+    sim.step(999)
+    ref.step(999)
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(rho, r_rho) <= 1e-4
+    assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= 1e-4
+
+
+def test_shear_wave_decay_matches_viscosity(gpu):
+    """Periodic shear wave u_x = U sin(2 pi y / ny) decays as exp(-nu k^2 t), nu = (tau - 1/2)/3."""
+    nx, ny, tau, U, steps = 64, 128, 0.8, 0.01, 2000
+    sim = FluidSimulator(nx, ny, mode="physics", dtype="f64", scene="periodic", tau=tau)
+    y = np.arange(ny)
+    ux = np.tile((U * np.sin(2 * np.pi * y / ny))[:, None], (1, nx))
+    sim.init_equilibrium(None, ux, None)
+    sim.step(steps)
+    _, ux1, _ = sim.read_macro()
+    amp = 2.0 * np.mean(ux1 * np.sin(2 * np.pi * y / ny)[:, None])
+    nu = (tau - 0.5) / 3.0
+    k = 2 * np.pi / ny
+    expected = U * np.exp(-nu * k * k * steps)
+    assert abs(amp - expected) / expected < 5e-3
+
+
+def test_precision_forms_against_fp64(gpu):
+    nx, ny = 256, 128
+    kw = dict(mode="physics", scene="channel", tau=0.6, inlet_speed=0.05, seed=3, disk_radius=(5.0, 10.0))
+    ref = FluidSimulator(nx, ny, dtype="f64", **kw)
+    ref.step(2000)
+    errs = {}
+    for dt in ("f32", "f16", "bf16"):
+        s = FluidSimulator(nx, ny, dtype=dt, **kw)
+        s.step(2000)
+        errs[dt] = s.macro_error(ref)
+        assert s.nonfinite_count() == 0
+    assert errs["f32"][1] < 1e-5
+    assert errs["f16"][1] < 1e-3
+    assert errs["bf16"][1] < 2e-2
+
+
+def test_init_equilibrium_roundtrip(gpu):
+    nx, ny = 80, 60
+    rng = np.random.default_rng(5)
+    rho = (1.0 + 0.01 * rng.standard_normal((ny, nx))).astype(np.float32)
+    ux = (0.03 * rng.standard_normal((ny, nx))).astype(np.float32)
+    uy = (0.03 * rng.standard_normal((ny, nx))).astype(np.float32)
+    sim = FluidSimulator(nx, ny, mode="physics", scene="periodic", tau=0.7)
+    sim.init_equilibrium(rho, ux, uy)
+    f = sim.read_populations(np.float64)
+    ex = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])[:, None, None]
+    ey = np.array([0, 0, -1, 0, 1, -1, -1, 1, 1])[:, None, None]
+    r = f.sum(0)
+    assert np.max(np.abs(r - rho)) < 1e-6
+    assert np.max(np.abs((ex * f).sum(0) / r - ux)) < 1e-6
+    assert np.max(np.abs((ey * f).sum(0) / r - uy)) < 1e-6

@@ -1,0 +1,136 @@
+"""The C ABI without a GPU: the library loads, exports every declared symbol, validates
+arguments without aborting, and its host-side mask logic (masks, obstacle discs, force
+strokes) agrees with the oracle's restatement of lattice.rs / d2q9_node.rs."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ROOT
+
+
+def _declared(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lbm_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(native):
+    names = _declared("lbm.h")
+    assert len(names) > 30
+    missing = [n for n in names if not hasattr(native, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_defaults(native):
+    from simuverse_gb300 import _native as nat
+
+    assert native.lbm_abi_version() == 1
+    p = nat.LbmParams()
+    native.lbm_params_default(ctypes.byref(p))
+    assert (p.nx, p.ny) == (600, 375)  # 1200x750 canvas, lattice_pixel_size 2
+    assert p.tau == pytest.approx(0.56)
+    assert p.lid_speed == pytest.approx(0.13) and p.inlet_speed == pytest.approx(0.12)
+
+
+@pytest.mark.parametrize("field,value", [("nx", 2), ("ny", 70000), ("mode", 5), ("dtype", 9), ("scene", 3),
+                                         ("tau", 0.0), ("pixel_size", 0)])
+def test_create_rejects_bad_params(native, field, value):
+    from simuverse_gb300 import _native as nat
+
+    p = nat.LbmParams()
+    native.lbm_params_default(ctypes.byref(p))
+    setattr(p, field, value)
+    h = ctypes.c_void_p()
+    rc = native.lbm_create(ctypes.byref(p), ctypes.byref(h))
+    assert rc == nat.LBM_ERR_ARG
+    assert h.value is None
+    assert len(native.lbm_last_error()) > 0
+
+
+def test_null_handles_are_errors(native):
+    from simuverse_gb300 import _native as nat
+
+    assert native.lbm_step(None, 1) == nat.LBM_ERR_ARG
+    assert native.lbm_reset(None) == nat.LBM_ERR_ARG
+    assert native.lbm_destroy(None) == nat.LBM_OK
+    assert native.lbm_create(None, None) == nat.LBM_ERR_ARG
+
+
+def _mask(native, nx, ny, mode, scene, **kw):
+    from simuverse_gb300 import _native as nat
+
+    p = nat.LbmParams()
+    native.lbm_params_default(ctypes.byref(p))
+    p.nx, p.ny, p.mode, p.scene = nx, ny, mode, scene
+    for k, v in kw.items():
+        setattr(p, k, v)
+    out = np.zeros((ny, nx), nat.INFO_DTYPE)
+    nat.check(native.lbm_build_mask(ctypes.byref(p), nat.ptr(out)))
+    return out
+
+
+@pytest.mark.parametrize("scene,nx,ny", [("poiseuille", 600, 375), ("poiseuille", 97, 61), ("cavity", 256, 256),
+                                         ("custom", 17, 9)])
+def test_reference_masks_match_oracle(native, scene, nx, ny):
+    sc = {"poiseuille": 0, "cavity": 1, "custom": 2}[scene]
+    got = _mask(native, nx, ny, 0, sc, lid_speed=0.1, inlet_speed=0.12)
+    assert np.array_equal(got, oracle.mask_reference(nx, ny, scene, 0.1, 0.12))
+
+
+def test_physics_masks_match_oracle(native):
+    assert np.array_equal(_mask(native, 130, 70, 1, 1, lid_speed=0.1), oracle.mask_physics_cavity(130, 70, 0.1))
+    for seed in (0, 1, 1234):
+        got = _mask(native, 700, 300, 1, 3, inlet_speed=0.05, seed=seed, solid_fraction=0.05,
+                    disk_rmin=8.0, disk_rmax=32.0)
+        ref, _ = oracle.mask_physics_channel(700, 300, 0.05, seed, 0.05, 8.0, 32.0)
+        assert np.array_equal(got, ref)
+
+
+def test_obstacle_disc_matches_oracle(native):
+    from simuverse_gb300 import _native as nat
+
+    nx, ny = 200, 150
+    base = oracle.mask_reference(nx, ny, "cavity")
+    for x, y in ((100, 70), (28, 28), (171, 121), (0, 40)):
+        a = base.copy()
+        nat.check(native.lbm_mask_add_obstacle(nx, ny, nat.ptr(a), x, y))
+        host, dev = base.copy(), base.copy()
+        assert oracle.lib().lo_add_obstacle(nx, ny, oracle._p(host), oracle._p(dev), x, y) == 0
+        assert np.array_equal(a, host) and np.array_equal(a, dev)
+    bad = base.copy()
+    assert native.lbm_mask_add_obstacle(nx, ny, nat.ptr(bad), 100, 10) == nat.LBM_ERR_ARG
+
+
+@pytest.mark.parametrize("pos,pre,ps", [((400.0, 300.0), (380.0, 290.0), 4), ((100.0, 100.0), (120.0, 60.0), 2),
+                                        ((5.0, 5.0), (50.0, 40.0), 3), ((790.0, 10.0), (700.0, 50.0), 4),
+                                        ((300.0, 300.0), (300.0, 300.0), 4)])
+def test_force_stroke_matches_oracle(native, pos, pre, ps):
+    from simuverse_gb300 import _native as nat
+
+    nx, ny = 200, 150
+    a = oracle.mask_reference(nx, ny, "poiseuille")
+    b = a.copy()
+    n = native.lbm_mask_force_stroke(nx, ny, ps, nat.ptr(a), pos[0], pos[1], pre[0], pre[1])
+    assert n >= 0
+    oracle.lib().lo_add_external_force(nx, ny, ps, oracle._p(b), pos[0], pos[1], pre[0], pre[1])
+    assert np.array_equal(a, b)
+
+
+def test_force_stroke_rejects_unit_pixel(native):
+    from simuverse_gb300 import _native as nat
+
+    a = oracle.mask_reference(50, 40, "cavity")
+    assert native.lbm_mask_force_stroke(50, 40, 1, nat.ptr(a), 10.0, 10.0, 20.0, 20.0) == nat.LBM_ERR_ARG
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    from simuverse_gb300 import _native as nat
+
+    monkeypatch.setattr(nat, "_lib", None)
+    monkeypatch.setattr(nat, "LIB_PATH", str(tmp_path / "absent.so"))
+    with pytest.raises(RuntimeError):
+        nat.load()

@@ -1,0 +1,109 @@
+"""The oracle itself: pinned to the golden fixtures of the independent pure-Python
+restatement, and checked on analytic physics cases.  CPU only."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN
+
+FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=os.path.basename)
+def test_oracle_matches_golden(path):
+    z = np.load(path)
+    scene = str(z["scene"])
+    ny, nx = z["info_in"].shape
+    kw = {}
+    if scene == "cavity":
+        kw["lid_vx"] = float(z["speed"])
+    if scene == "poiseuille":
+        kw["inlet_vx"] = float(z["speed"])
+    o = oracle.RefOracle(nx, ny, scene, tau=float(z["tau"]), **kw)
+    assert np.array_equal(o.host_info, z["info_in"])  # lattice.rs mask
+    o.info[...] = z["info_init"]
+    for s in range(int(z["steps"])):
+        if str(z["edit"]) == "obstacle" and s == 2:
+            assert o.add_obstacle(32, 30) == 0
+        o.step()
+    assert np.array_equal(o.populations, z["pops"])
+    assert np.array_equal(o.macro4, z["macro"])
+    assert np.array_equal(o.info, z["info_out"])
+
+
+def test_golden_fixtures_exist():
+    assert len(FIXTURES) >= 4
+
+
+def test_pyref_masks_match_oracle():
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    import pyref
+
+    for scene, nx, ny in (("poiseuille", 200, 120), ("cavity", 33, 21), ("custom", 9, 7), ("poiseuille", 600, 375)):
+        assert np.array_equal(pyref.mask(nx, ny, scene), oracle.mask_reference(nx, ny, scene))
+
+
+def test_physics_f64_mass_exact_in_closed_cavity():
+    p = oracle.PhysOracle(oracle.mask_physics_cavity(64, 48, 0.1), 0.6, np.float64)
+    m0 = p.conservation()[0]
+    p.step(500)
+    assert abs(p.conservation()[0] - m0) / m0 < 1e-13
+
+
+def test_physics_f32_mass_drift_bounded():
+    p = oracle.PhysOracle(oracle.mask_physics_cavity(128, 128, 0.1), 0.6, np.float32)
+    m0 = p.conservation()[0]
+    p.step(1000)
+    assert abs(p.conservation()[0] - m0) / m0 < 1e-10
+
+
+def test_rest_state_is_invariant():
+    info = oracle.mask_physics_channel(128, 64, 0.0, 1, 0.05, 4.0, 8.0)[0]
+    p = oracle.PhysOracle(info, 0.7, np.float64)
+    p.step(50)
+    assert np.max(np.abs(p.deviations)) < 1e-15
+
+
+def test_shear_wave_decay_rate():
+    nx, ny, tau, U, steps = 32, 128, 0.8, 0.01, 2000
+    p = oracle.PhysOracle(oracle.mask_periodic(nx, ny), tau, np.float64)
+    y = np.arange(ny)
+    p.init_equilibrium(None, np.tile((U * np.sin(2 * np.pi * y / ny))[:, None], (1, nx)), None)
+    p.step(steps)
+    _, ux, _ = p.macro()
+    amp = 2.0 * np.mean(ux * np.sin(2 * np.pi * y / ny)[:, None])
+    expected = U * np.exp(-(tau - 0.5) / 3.0 * (2 * np.pi / ny) ** 2 * steps)
+    assert abs(amp - expected) / expected < 2e-3
+
+
+def test_poiseuille_channel_profile():
+    """Empty channel: the Zou-He parabolic inlet profile is carried to the outlet."""
+    nx, ny = 96, 34
+    info, nd = oracle.mask_physics_channel(nx, ny, 0.04, 1, 0.0, 8.0, 8.0)
+    assert nd == 0
+    p = oracle.PhysOracle(info, 0.8, np.float64)
+    p.step(6000)
+    _, ux, _ = p.macro()
+    H = ny - 2
+    s = np.arange(1, ny - 1) - 0.5
+    expected = 4 * 0.04 * s * (H - s) / H**2
+    prof = ux[1:-1, nx // 2]
+    assert np.max(np.abs(prof - expected)) / 0.04 < 0.02
+
+
+def test_channel_mask_properties():
+    nx, ny = 1024, 512
+    a, nd = oracle.mask_physics_channel(nx, ny, 0.05, 42, 0.05, 8.0, 32.0)
+    b, nd2 = oracle.mask_physics_channel(nx, ny, 0.05, 42, 0.05, 8.0, 32.0)
+    c, _ = oracle.mask_physics_channel(nx, ny, 0.05, 43, 0.05, 8.0, 32.0)
+    assert nd == nd2 and np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+    frac = (a["material"] == 4).mean()
+    assert 0.05 <= frac < 0.06
+    assert (a["material"][:, 0] == 3)[1:-1].all() and (a["material"][:, -1] == 5)[1:-1].all()
+    assert (a["material"][0] == 2).all() and (a["material"][-1] == 2).all()
