@@ -72,6 +72,11 @@ extern "C" {
 #define LBM_DTYPE_F16 2  /* physics mode only: (f_i - w_i) * 2^10 in FP16, FP32 arithmetic */
 #define LBM_DTYPE_BF16 3 /* physics mode only: f_i - w_i in BF16, FP32 arithmetic */
 
+/* step kernel variants (physics mode) */
+#define LBM_KERNEL_AUTO 0   /* four cells per thread when nx % 4 == 0, else one */
+#define LBM_KERNEL_CELL 1   /* one cell per thread */
+#define LBM_KERNEL_VEC4 2   /* four cells per thread, vector loads and stores (nx % 4 == 0) */
+
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */
 #define LBM_SCENE_CAVITY 1     /* lattice.rs:52-61 (reference); moving-lid box (physics) */
@@ -111,7 +116,8 @@ typedef struct lbm_params {
     int32_t pixel_size;      /* canvas pixels per lattice cell for on_click/touch_move */
     int32_t macro_every_step;/* 1: write the macro field every step, as the reference does;
                                 0: only on the last step of each lbm_step call */
-    int32_t reserved[6];
+    int32_t kernel;          /* LBM_KERNEL_*: step kernel variant (results agree to rounding) */
+    int32_t reserved[5];
 } lbm_params;
 
 typedef struct lbm_handle lbm_handle;

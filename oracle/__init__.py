@@ -181,10 +181,11 @@ class PhysOracle:
         self.init_equilibrium()
 
     def set_tau(self, tau):
+        # the library takes tau as FP32; FP64 runs use 1 / double(tau)
         if self.dtype == np.float32:
             self.omega = float(np.float32(1.0) / np.float32(tau))
         else:
-            self.omega = 1.0 / float(tau)
+            self.omega = 1.0 / float(np.float32(tau))
 
     def _sfx(self):
         return "f32" if self.dtype == np.float32 else "f64"

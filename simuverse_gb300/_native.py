@@ -26,6 +26,7 @@ LBM_ERR_NOMEM = -7
 MODES = {"reference": 0, "physics": 1}
 DTYPES = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4}
+KERNELS = {"auto": 0, "cell": 1, "vec4": 2}
 BULK, BOUNDARY, INLET, OBSTACLE, OUTLET, EXTERNAL_FORCE, GHOST = 1, 2, 3, 4, 5, 6, 7
 
 # LatticeInfo (simuverse/src/fluid/lattice.rs:5-13)
@@ -40,7 +41,7 @@ class LbmParams(ctypes.Structure):
         ("solid_fraction", ctypes.c_float), ("disk_rmin", ctypes.c_float), ("disk_rmax", ctypes.c_float),
         ("seed", ctypes.c_uint64),
         ("pixel_size", ctypes.c_int32), ("macro_every_step", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
     ]
 
 

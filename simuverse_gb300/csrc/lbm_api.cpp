@@ -228,6 +228,9 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "scene %d exists in physics mode only", p.scene);
     if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
+    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_VEC4) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if (p.kernel == LBM_KERNEL_VEC4 && (p.mode != LBM_MODE_PHYSICS || p.nx % 4 != 0))
+        return fail(LBM_ERR_ARG, "the four-cell kernel needs physics mode and nx %% 4 == 0");
     if (p.scene == LBM_SCENE_CHANNEL && !(p.disk_rmin >= 0.0f && p.disk_rmax >= p.disk_rmin && p.solid_fraction >= 0.0f &&
                                          p.solid_fraction < 0.5f))
         return fail(LBM_ERR_ARG, "channel disk parameters out of range");
@@ -327,6 +330,7 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
     h->fluid_ty = (p.scene == LBM_SCENE_CAVITY) ? 1 : 0;
     h->tau = p.tau;
     h->omega = 1.0f / p.tau;
+    h->omega_d = 1.0 / (double)p.tau;
     cudaError_t e = cudaGetDevice(&h->device);
     const size_t pop_bytes = 9 * h->N * lbm::dtype_size(p.dtype);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
@@ -425,6 +429,7 @@ int lbm_set_tau(lbm_handle* h, float tau) {
     if (!(tau > 0.0f) || !std::isfinite(tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     h->tau = tau;
     h->omega = 1.0f / tau;  // mod.rs:35
+    h->omega_d = 1.0 / (double)tau;
     return LBM_OK;
 }
 
@@ -751,6 +756,7 @@ int lbm_load(lbm_handle* h, const char* path) {
     h->cur = hd.cur & 1;
     h->tau = hd.tau;
     h->omega = 1.0f / hd.tau;
+    h->omega_d = 1.0 / (double)hd.tau;
     h->pre_x = hd.pre_x;
     h->pre_y = hd.pre_y;
     h->stepped_since_init = hd.stepped != 0;

@@ -47,6 +47,12 @@ constexpr unsigned FL_MOVING = 1u << 13;
 
 __host__ __device__ constexpr bool is_solid(int m) { return m == LBM_BOUNDARY || m == LBM_OBSTACLE; }
 
+// round-to-nearest add and multiply that the compiler may not contract into an FMA
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 // ---- population storage formats ------------------------------------------------
 // R: arithmetic type; T: stored type.  Physics-mode storage holds d = f - w (shifted
 // deviation); FP16 additionally scales by 2^10 so that small deviations stay normal.

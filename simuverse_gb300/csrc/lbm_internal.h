@@ -17,6 +17,7 @@ struct lbm_handle {
     size_t N = 0;
     int fluid_ty = 0;  // d2q9_node.rs:53-57: 1 for the cavity, else 0
     float tau = 0.6f, omega = 1.0f / 0.6f;
+    double omega_d = 1.0 / (double)0.6f;  // 1 / tau in FP64, for FP64 storage
     void* buf[2] = {nullptr, nullptr};  // ping-pong population buffers (9*N each)
     int cur = 0;                        // buffer holding the state the next step reads
     uint16_t* d_flags = nullptr;
@@ -48,6 +49,9 @@ cudaError_t launch_ref_init(lbm_handle* h, cudaStream_t s);
 cudaError_t launch_phys_init(lbm_handle* h, const float* d_rho, const float* d_ux, const float* d_uy,
                              cudaStream_t s);
 cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s);
+// four-cells-per-thread physics step (lbm_step_vec.cu)
+bool vec_step_supported(const lbm_handle* h);
+cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s);
 cudaError_t launch_conservation(lbm_handle* h, double* d_out3, cudaStream_t s);
 cudaError_t launch_count_nonfinite(lbm_handle* h, cudaStream_t s);
 cudaError_t launch_macro_error(lbm_handle* h, lbm_handle* ref, double* d_out4, cudaStream_t s);

@@ -17,6 +17,7 @@
 // round-to-nearest intrinsics (no multiply-add contraction), so it agrees bit for bit with
 // a CPU restatement compiled with contraction off.  Physics mode is a standard BGK step
 // with exact weights, stored as deviations f - w.
+#include "lbm_cell.cuh"
 #include "lbm_common.cuh"
 #include "lbm_internal.h"
 
@@ -223,105 +224,16 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
 }
 
 // ------------------------------------------------------------------------------------
-// physics-mode step
+// physics-mode step (cell update in lbm_cell.cuh)
 // ------------------------------------------------------------------------------------
 template <class ST, bool MACRO>
 __global__ void __launch_bounds__(TPB) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                    typename ST::R omega, int nx, int ny, float* __restrict__ macro) {
-    using R = typename ST::R;
     const int x = blockIdx.x * TPB + threadIdx.x;
     const int y = blockIdx.y;
     if (x >= nx) return;
-    const size_t N = (size_t)nx * ny;
-    const size_t c = (size_t)y * nx + x;
-    const unsigned fl = flags[c];
-    const int m = (int)(fl & FL_MAT_MASK);
-    if (is_solid(m)) {
-        if (MACRO) { macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f; }
-        return;
-    }
-    const bool outlet = (m == LBM_OUTLET);
-    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
-    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
-    R d[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
-        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        if (fl & (1u << (FL_DIR_SHIFT + j))) {
-            R v = ST::ld(A + c + (size_t)INV(j) * N);  // half-way bounce-back
-            if (fl & FL_MOVING) {
-                const lbm_lattice_info si = info[row + sx];
-                const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
-                if (uw != R(0)) v = v + R(6) * PW<R>(j) * uw;
-            }
-            d[j] = v;
-        } else {
-            d[j] = ST::ld(A + row + sx + (size_t)j * N);
-        }
-    }
-    if (m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
-        const lbm_lattice_info in = info[c];
-        const R ux = R(in.vx), uy = R(in.vy);
-        const R S = d[0] + d[2] + d[4] + R(2) * (d[3] + d[6] + d[7]);
-        const R rho = (R(1) + S) / (R(1) - ux);
-        const R rux = rho * ux, ruy = rho * uy;
-        d[1] = d[3] + (R(2) / R(3)) * rux;
-        d[5] = d[7] + R(0.5) * (d[4] - d[2]) + rux / R(6) - R(0.5) * ruy;
-        d[8] = d[6] + R(0.5) * (d[2] - d[4]) + rux / R(6) + R(0.5) * ruy;
-    }
-    if (outlet) {  // zero-gradient outflow anchored at rho = 1: f_j <- f_j / rho
-        const R dr = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
-        const R inv = R(1) / (R(1) + dr);
-#pragma unroll
-        for (int j = 0; j < 9; ++j) d[j] = (d[j] - PW<R>(j) * dr) * inv;
-    }
-    const R drho = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
-    R jx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
-    R jy = (d[4] - d[2]) + (d[7] - d[5]) + (d[8] - d[6]);
-    const R rho = R(1) + drho;
-    R Fx = R(0), Fy = R(0);
-    const bool forced = (m == LBM_EXTERNAL_FORCE);
-    if (forced) {  // Guo forcing with the reference's block_iter countdown
-        lbm_lattice_info in = info[c];
-        if (in.block_iter > 0) {
-            in.block_iter = in.block_iter - 1;
-            if (in.block_iter == 0) {
-                in.material = LBM_BULK;
-                flags[c] = (uint16_t)((fl & ~FL_MAT_MASK) | LBM_BULK);
-            }
-            info[c] = in;
-        }
-        Fx = R(in.vx);
-        Fy = R(in.vy);
-        jx = jx + R(0.5) * Fx;
-        jy = jy + R(0.5) * Fy;
-    }
-    const R ux = jx / rho, uy = jy / rho;
-    if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
-    const R usq = R(1.5) * (ux * ux + uy * uy);
-    const R gf = R(1) - R(0.5) * omega;
-    R o[9];
-#pragma unroll
-    for (int j = 1; j < 9; ++j) {
-        const R ex = R(EX(j)), ey = R(EY(j));
-        const R eu = ex * ux + ey * uy;
-        const R deq = PW<R>(j) * (drho + rho * (R(3) * eu + R(4.5) * (eu * eu) - usq));
-        R out = d[j] - omega * (d[j] - deq);
-        if (forced) {
-            const R eF = ex * Fx + ey * Fy;
-            const R uF = ux * Fx + uy * Fy;
-            out = out + gf * PW<R>(j) * (R(3) * (eF - uF) + R(9) * eu * eF);
-        }
-        o[j] = out;
-    }
-    // rest population from mass conservation: sum_j o_j = drho by construction (the BGK
-    // value in exact arithmetic; removes the bias of the rounded weights' moments)
-    o[0] = drho - (((o[1] + o[3]) + (o[2] + o[4])) + ((o[5] + o[7]) + (o[6] + o[8])));
-#pragma unroll
-    for (int j = 0; j < 9; ++j) ST::st(B + c + (size_t)j * N, o[j]);
+    phys_cell_update<ST, MACRO>(A, B, flags, info, omega, x, y, nx, ny, macro);
 }
 
 // ------------------------------------------------------------------------------------
@@ -534,8 +446,10 @@ cudaError_t launch_phys_init(lbm_handle* h, const float* r, const float* ux, con
 template <class ST, bool MACRO>
 static cudaError_t phys_step_t(lbm_handle* h, cudaStream_t s) {
     using T = typename ST::T;
+    using R = typename ST::R;
+    const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     k_phys_step<ST, MACRO><<<cell_grid(h), TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, (typename ST::R)h->omega, h->nx, h->ny, h->d_macro);
+                                                        h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
 }
 
@@ -549,6 +463,7 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
             k_ref_step<false><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
         return cudaGetLastError();
     }
+    if (h->p.kernel != LBM_KERNEL_CELL && vec_step_supported(h)) return launch_phys_step_vec(h, write_macro, s);
     switch (h->p.dtype) {
         case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
         case LBM_DTYPE_F64: return write_macro ? phys_step_t<StoreF64, true>(h, s) : phys_step_t<StoreF64, false>(h, s);
