@@ -37,14 +37,14 @@ UNIT = "GLUPS"
 
 def workload_params(args):
     return dict(nx=args.nx, ny=args.ny, mode="physics", dtype=args.dtype, scene="channel", tau=0.56,
-                inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0), seed=1234)
+                inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0), seed=1234, kernel=args.kernel)
 
 
 def config_dict(args):
     return {"workload": "channel %dx%d %s, Zou-He inlet u=0.05 parabolic, outflow, walls, disks r 8-32 5%% solid, "
                         "tau 0.56, equilibrium start" % (args.nx, args.ny, args.dtype),
             "cells": args.nx * args.ny, "steps_per_bench_step": 1, "l2_flush": "none: working set 1.2 GB > L2",
-            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU", "kernel": args.kernel}
 
 
 def dist_env():
@@ -303,6 +303,7 @@ def main():
     ap.add_argument("--ny", type=int, default=4096)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -76,6 +76,8 @@ extern "C" {
 #define LBM_KERNEL_AUTO 0   /* four cells per thread when nx % 4 == 0, else one */
 #define LBM_KERNEL_CELL 1   /* one cell per thread */
 #define LBM_KERNEL_VEC4 2   /* four cells per thread, vector loads and stores (nx % 4 == 0) */
+#define LBM_KERNEL_BULK 3   /* four cells per thread fed by double-buffered bulk asynchronous
+                               copies into shared memory, persistent blocks (nx % 8 == 0) */
 
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */
@@ -199,6 +201,10 @@ int lbm_macro_error(lbm_handle* h, lbm_handle* ref, double out[4]);
 int lbm_save(lbm_handle* h, const char* path);
 int lbm_load(lbm_handle* h, const char* path);
 
+/* synchronises; LBM_ERR_TIMEOUT if a step kernel gave up on a bounded wait since creation
+   -- no counterpart in the reference */
+int lbm_status(lbm_handle* h);
+
 /* counters -- no counterpart in the reference */
 int lbm_steps_done(const lbm_handle* h, uint64_t* steps);
 int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches);
@@ -207,6 +213,64 @@ int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches);
    macro: 3 planes of N floats (rho, ux, uy).  No counterpart in the reference, whose
    consumers bind macro_tex directly. */
 int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy);
+
+/* ---------------------------------------------------------------------------------
+   Batched form -- no counterpart in the reference (simuverse runs one lattice).  Many
+   independent physics-mode FP32 lattices (moving-lid cavities and channels) of uneven
+   size advance together: in one cooperative persistent launch per lbm_batch_step call,
+   replayed from a CUDA graph (LBM_BATCH_PERSISTENT), in one tile-list launch per step
+   (LBM_BATCH_TILE_LAUNCHES), or in one launch per domain and step
+   (LBM_BATCH_DOMAIN_LOOP).  The persistent kernel's grid barrier waits at most a set time;
+   a timed-out wait sets an error that lbm_batch_status returns as LBM_ERR_TIMEOUT.
+   --------------------------------------------------------------------------------- */
+#define LBM_BATCH_PERSISTENT 0
+#define LBM_BATCH_TILE_LAUNCHES 1
+#define LBM_BATCH_DOMAIN_LOOP 2
+
+typedef struct lbm_domain_desc {
+    int32_t nx, ny;
+    int32_t scene;  /* LBM_SCENE_CAVITY (lid at row 0 moving at speed) or LBM_SCENE_CHANNEL
+                       (parabolic Zou-He inlet of peak speed, outflow, walls) */
+    float tau;
+    float speed;
+    int32_t reserved[3];
+} lbm_domain_desc;
+
+typedef struct lbm_batch_config {
+    int32_t tile_threads_x; /* threads per tile row (multiple of 32); a tile is 4x that wide */
+    int32_t tile_rows;      /* rows per tile (threads per block = tile_threads_x * tile_rows <= 256) */
+    int32_t blocks_per_sm;  /* persistent grid = blocks_per_sm x SMs (0: occupancy maximum) */
+    int32_t method;         /* LBM_BATCH_* */
+    float ms_per_step;      /* filled by lbm_batch_tune */
+    int32_t reserved[3];
+} lbm_batch_config;
+
+typedef struct lbm_batch lbm_batch;
+
+/* the seeded domain list: nx log-uniform in [64, 1024], ny = nx * aspect with aspect
+   U[0.5, 2] (redrawn until ny is in [64, 1024]), tau U[0.55, 1], speed U[0.02, 0.1],
+   cavity or channel with probability 1/2 (mt19937_64(seed)) */
+int lbm_batch_generate(int32_t n, uint64_t seed, lbm_domain_desc* out);
+int lbm_batch_create(int32_t n, const lbm_domain_desc* domains, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* b);
+int lbm_batch_set_stream(lbm_batch* b, void* cuda_stream);
+int lbm_batch_info(const lbm_batch* b, int32_t* ndomains, uint64_t* cells);
+int lbm_batch_set_config(lbm_batch* b, const lbm_batch_config* cfg);
+int lbm_batch_get_config(const lbm_batch* b, lbm_batch_config* cfg);
+/* times trial_steps of every candidate tile shape and grid size, keeps the fastest
+   (cached per shape class for the life of the process) */
+int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best);
+int lbm_batch_step(lbm_batch* b, int32_t nsteps);
+/* synchronises; LBM_ERR_TIMEOUT if a persistent launch's grid barrier timed out */
+int lbm_batch_status(lbm_batch* b);
+/* failure injection: a persistent launch in which `block` leaves before the barrier of
+   `step`; the others time out after timeout_ns (0: the default 1 s).  Returns the status. */
+int lbm_batch_inject_missing_arrival(lbm_batch* b, int32_t nsteps, int32_t block, int32_t step, uint64_t timeout_ns);
+int lbm_batch_read_macro(lbm_batch* b, int32_t i, float* rho, float* ux, float* uy);
+int lbm_batch_read_populations(lbm_batch* b, int32_t i, float* f);
+int lbm_batch_read_info(lbm_batch* b, int32_t i, lbm_lattice_info* info);
+int lbm_batch_conservation(lbm_batch* b, int32_t i, double out[3]);
+int lbm_batch_counters(const lbm_batch* b, uint64_t* steps, uint64_t* launches);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,7 @@ LBM_ERR_NOMEM = -7
 MODES = {"reference": 0, "physics": 1}
 DTYPES = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4}
-KERNELS = {"auto": 0, "cell": 1, "vec4": 2}
+KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3}
 BULK, BOUNDARY, INLET, OBSTACLE, OUTLET, EXTERNAL_FORCE, GHOST = 1, 2, 3, 4, 5, 6, 7
 
 # LatticeInfo (simuverse/src/fluid/lattice.rs:5-13)
@@ -43,6 +43,20 @@ class LbmParams(ctypes.Structure):
         ("pixel_size", ctypes.c_int32), ("macro_every_step", ctypes.c_int32),
         ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
     ]
+
+
+class DomainDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("scene", ctypes.c_int32),
+                ("tau", ctypes.c_float), ("speed", ctypes.c_float), ("reserved", ctypes.c_int32 * 3)]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("tile_threads_x", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32), ("method", ctypes.c_int32),
+                ("ms_per_step", ctypes.c_float), ("reserved", ctypes.c_int32 * 3)]
+
+
+BATCH_METHODS = {"persistent": 0, "tile_launches": 1, "domain_loop": 2}
 
 
 class LbmError(RuntimeError):
@@ -88,9 +102,26 @@ _SIGNATURES = {
     "lbm_macro_error": [_P, _P, ctypes.POINTER(_D)],
     "lbm_save": [_P, ctypes.c_char_p],
     "lbm_load": [_P, ctypes.c_char_p],
+    "lbm_status": [_P],
     "lbm_steps_done": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_kernel_launches": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_device_macro": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "lbm_batch_generate": [_I, ctypes.c_uint64, _P],
+    "lbm_batch_create": [_I, _P, ctypes.POINTER(_P)],
+    "lbm_batch_destroy": [_P],
+    "lbm_batch_set_stream": [_P, _P],
+    "lbm_batch_info": [_P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_uint64)],
+    "lbm_batch_set_config": [_P, _P],
+    "lbm_batch_get_config": [_P, _P],
+    "lbm_batch_tune": [_P, _I, _P],
+    "lbm_batch_step": [_P, _I],
+    "lbm_batch_status": [_P],
+    "lbm_batch_inject_missing_arrival": [_P, _I, _I, _I, ctypes.c_uint64],
+    "lbm_batch_read_macro": [_P, _I, _P, _P, _P],
+    "lbm_batch_read_populations": [_P, _I, _P],
+    "lbm_batch_read_info": [_P, _I, _P],
+    "lbm_batch_conservation": [_P, _I, ctypes.POINTER(_D)],
+    "lbm_batch_counters": [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
 }
 
 _lib = None

@@ -228,9 +228,11 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "scene %d exists in physics mode only", p.scene);
     if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
-    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_VEC4) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_BULK) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
     if (p.kernel == LBM_KERNEL_VEC4 && (p.mode != LBM_MODE_PHYSICS || p.nx % 4 != 0))
         return fail(LBM_ERR_ARG, "the four-cell kernel needs physics mode and nx %% 4 == 0");
+    if (p.kernel == LBM_KERNEL_BULK && (p.mode != LBM_MODE_PHYSICS || p.nx % 8 != 0))
+        return fail(LBM_ERR_ARG, "the bulk-copy kernel needs physics mode and nx %% 8 == 0");
     if (p.scene == LBM_SCENE_CHANNEL && !(p.disk_rmin >= 0.0f && p.disk_rmax >= p.disk_rmin && p.solid_fraction >= 0.0f &&
                                          p.solid_fraction < 0.5f))
         return fail(LBM_ERR_ARG, "channel disk parameters out of range");
@@ -280,6 +282,7 @@ void free_all(lbm_handle* h) {
     cudaFree(h->d_macro);
     cudaFree(h->d_part);
     cudaFree(h->d_count);
+    cudaFree(h->d_status);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
@@ -289,6 +292,13 @@ int check_handle(const lbm_handle* h) {
 }
 
 }  // namespace
+
+namespace lbm {
+int set_error(int code, const char* msg) {
+    g_err = msg;
+    return code;
+}
+}  // namespace lbm
 
 extern "C" {
 
@@ -342,6 +352,8 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_macro, 3 * h->N * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_part, (size_t)lbm::RED_BLOCKS * 6 * sizeof(double) + 64 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_count, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
         free_all(h);
         delete h;
@@ -765,6 +777,16 @@ int lbm_load(lbm_handle* h, const char* path) {
     h->fluid_ty = hd.fluid_ty;
     LBM_TRY(rebuild_flags(h));
     return sync(h);
+}
+
+int lbm_status(lbm_handle* h) {
+    LBM_TRY(check_handle(h));
+    LBM_TRY(use_device(h));
+    int st = 0;
+    LBM_CK(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    LBM_TRY(sync(h));
+    if (st != 0) return fail(st, "a step kernel gave up on a bounded wait (status %d)", st);
+    return LBM_OK;
 }
 
 int lbm_steps_done(const lbm_handle* h, uint64_t* steps) {

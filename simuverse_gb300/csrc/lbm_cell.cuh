@@ -37,9 +37,9 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
 #pragma unroll
         for (int j = 0; j < 9; ++j) d[j] = (d[j] - PW<R>(j) * dr) * inv;
     }
-    const R drho = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
-    R jx = (d[1] - d[3]) + (d[5] - d[6]) + (d[8] - d[7]);
-    R jy = (d[4] - d[2]) + (d[7] - d[5]) + (d[8] - d[6]);
+    const R drho = d[0] + (((d[1] + d[3]) + (d[2] + d[4])) + ((d[5] + d[7]) + (d[6] + d[8])));
+    R jx = (d[1] - d[3]) + ((d[5] - d[7]) + (d[8] - d[6]));
+    R jy = (d[4] - d[2]) + ((d[7] - d[5]) + (d[8] - d[6]));
     const R rho = R(1) + drho;
     R Fx = R(0), Fy = R(0);
     const bool forced = (m == LBM_EXTERNAL_FORCE);
@@ -58,22 +58,53 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
         jx = jx + R(0.5) * Fx;
         jy = jy + R(0.5) * Fy;
     }
-    const R ux = jx / rho, uy = jy / rho;
+    const R inv_rho = recip_rn(rho);
+    const R ux = jx * inv_rho, uy = jy * inv_rho;
     const R usq = R(1.5) * (ux * ux + uy * uy);
-    const R gf = R(1) - R(0.5) * omega;
-#pragma unroll
-    for (int j = 1; j < 9; ++j) {
-        const R ex = R(EX(j)), ey = R(EY(j));
-        const R eu = ex * ux + ey * uy;
-        const R deq = PW<R>(j) * (drho + rho * (R(3) * eu + R(4.5) * (eu * eu) - usq));
-        R out = d[j] - omega * (d[j] - deq);
-        if (forced) {
-            const R eF = ex * Fx + ey * Fy;
-            const R uF = ux * Fx + uy * Fy;
-            out = out + gf * PW<R>(j) * (R(3) * (eF - uF) + R(9) * eu * eF);
-        }
-        o[j] = out;
+    // BGK on opposite pairs (j, inv j): the equilibrium deviation splits into an even part
+    // w (drho + rho (4.5 (e.u)^2 - 1.5 u.u)) shared by the pair and an odd part 3 w rho e.u
+    const R om = omega, om1 = R(1) - omega;
+    const R r1 = rho * (R(3) * PW<R>(1)), r5 = rho * (R(3) * PW<R>(5));
+    {  // 1 / 3: e = (+-1, 0)
+        const R eu = ux;
+        const R sym = om * (PW<R>(1) * (drho + rho * (R(4.5) * eu * eu - usq)));
+        const R asy = om * (r1 * eu);
+        o[1] = om1 * d[1] + (sym + asy);
+        o[3] = om1 * d[3] + (sym - asy);
     }
+    {  // 4 / 2: e = (0, +-1)
+        const R eu = uy;
+        const R sym = om * (PW<R>(1) * (drho + rho * (R(4.5) * eu * eu - usq)));
+        const R asy = om * (r1 * eu);
+        o[4] = om1 * d[4] + (sym + asy);
+        o[2] = om1 * d[2] + (sym - asy);
+    }
+    {  // 8 / 6: e = +-(1, 1)
+        const R eu = ux + uy;
+        const R sym = om * (PW<R>(5) * (drho + rho * (R(4.5) * eu * eu - usq)));
+        const R asy = om * (r5 * eu);
+        o[8] = om1 * d[8] + (sym + asy);
+        o[6] = om1 * d[6] + (sym - asy);
+    }
+    {  // 5 / 7: e = +-(1, -1)
+        const R eu = ux - uy;
+        const R sym = om * (PW<R>(5) * (drho + rho * (R(4.5) * eu * eu - usq)));
+        const R asy = om * (r5 * eu);
+        o[5] = om1 * d[5] + (sym + asy);
+        o[7] = om1 * d[7] + (sym - asy);
+    }
+    if (forced) {
+        const R gf = R(1) - R(0.5) * omega;
+        const R uF = ux * Fx + uy * Fy;
+#pragma unroll
+        for (int j = 1; j < 9; ++j) {
+            const R eF = (EX(j) == 0 ? R(0) : R(EX(j)) * Fx) + (EY(j) == 0 ? R(0) : R(EY(j)) * Fy);
+            const R eu = (EX(j) == 0 ? R(0) : R(EX(j)) * ux) + (EY(j) == 0 ? R(0) : R(EY(j)) * uy);
+            o[j] = o[j] + gf * PW<R>(j) * (R(3) * (eF - uF) + R(9) * eu * eF);
+        }
+    }
+    // rest population from mass conservation: sum_j o_j = drho by construction (the BGK
+    // value in exact arithmetic; removes the bias of the rounded weights' moments)
     o[0] = drho - (((o[1] + o[3]) + (o[2] + o[4])) + ((o[5] + o[7]) + (o[6] + o[8])));
     rho_out = rho;
     ux_out = ux;
@@ -87,7 +118,7 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
                                                  float* __restrict__ macro) {
     using R = typename ST::R;
     const size_t N = (size_t)nx * ny;
-    const size_t c = (size_t)y * nx + x;
+    const unsigned c = (unsigned)y * (unsigned)nx + (unsigned)x;  // cells < 2^30
     const unsigned fl = flags[c];
     const int m = (int)(fl & FL_MAT_MASK);
     if (is_solid(m)) {
@@ -97,31 +128,40 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
     const bool outlet = (m == LBM_OUTLET);
     const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
     const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
+    const unsigned r0 = (unsigned)y * nx, rm = (unsigned)ym * nx, rp = (unsigned)yp * nx;
     R d[9];
+    if (!(fl & (0x1FEu << FL_DIR_SHIFT))) {  // no solid neighbour: plain pull
 #pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
-        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        if (fl & (1u << (FL_DIR_SHIFT + j))) {
-            R v = ST::ld(A + c + (size_t)INV(j) * N);  // half-way bounce-back
-            if (fl & FL_MOVING) {
-                const lbm_lattice_info si = info[row + sx];
-                const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
-                // rounded product, not an FMA: a contracted wall term leaves a
-                // systematic mass drift of ~1e-12 per step in FP32
-                if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j), uw));
+        for (int j = 0; j < 9; ++j) {
+            const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
+            const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+            d[j] = ST::ld(A + (size_t)j * N + (row + (unsigned)sx));
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
+            const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+            if (fl & (1u << (FL_DIR_SHIFT + j))) {
+                R v = ST::ld(A + (size_t)INV(j) * N + c);  // half-way bounce-back
+                if (fl & FL_MOVING) {
+                    const lbm_lattice_info si = info[row + sx];
+                    const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
+                    // rounded product, not an FMA: a contracted wall term leaves a
+                    // systematic mass drift of ~1e-12 per step in FP32
+                    if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j), uw));
+                }
+                d[j] = v;
+            } else {
+                d[j] = ST::ld(A + (size_t)j * N + (row + (unsigned)sx));
             }
-            d[j] = v;
-        } else {
-            d[j] = ST::ld(A + row + sx + (size_t)j * N);
         }
     }
     R o[9], rho, ux, uy;
     phys_collide<R>(d, m, fl, c, flags, info, omega, o, rho, ux, uy);
     if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
 #pragma unroll
-    for (int j = 0; j < 9; ++j) ST::st(B + c + (size_t)j * N, o[j]);
+    for (int j = 0; j < 9; ++j) ST::st(B + (size_t)j * N + c, o[j]);
 }
 
 }  // namespace lbm

@@ -52,6 +52,9 @@ __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, 
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+// correctly rounded reciprocal
+__device__ __forceinline__ float recip_rn(float a) { return __frcp_rn(a); }
+__device__ __forceinline__ double recip_rn(double a) { return __drcp_rn(a); }
 
 // ---- population storage formats ------------------------------------------------
 // R: arithmetic type; T: stored type.  Physics-mode storage holds d = f - w (shifted

@@ -26,6 +26,7 @@ struct lbm_handle {
     float* d_macro = nullptr;                 // rho, ux, uy planes
     double* d_part = nullptr;                 // reduction partials
     unsigned long long* d_count = nullptr;
+    int* d_status = nullptr;  // kernel status word (LBM_ERR_TIMEOUT from a bounded wait)
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     uint64_t steps = 0;
@@ -41,6 +42,9 @@ constexpr int TPB = 128;          // threads per block along x for the step kern
 constexpr int RED_BLOCKS = 1216;  // 8 x 152 SMs; fixed so FP64 sums have a fixed order
 constexpr int RED_TPB = 256;
 
+// records msg as the calling thread's lbm_last_error() and returns code
+int set_error(int code, const char* msg);
+
 inline size_t dtype_size(int dtype) { return dtype == LBM_DTYPE_F64 ? 8 : (dtype == LBM_DTYPE_F32 ? 4 : 2); }
 
 // Kernel launchers (lbm_kernels.cu).  All return cudaGetLastError() of the launch.
@@ -52,8 +56,13 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s);
 // four-cells-per-thread physics step (lbm_step_vec.cu)
 bool vec_step_supported(const lbm_handle* h);
 cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s);
+// bulk-copy fed physics step (lbm_step_bulk.cu)
+bool bulk_step_supported(const lbm_handle* h);
+cudaError_t launch_phys_step_bulk(lbm_handle* h, bool write_macro, cudaStream_t s);
 cudaError_t launch_conservation(lbm_handle* h, double* d_out3, cudaStream_t s);
 cudaError_t launch_count_nonfinite(lbm_handle* h, cudaStream_t s);
+cudaError_t launch_conservation_f32_phys(const float* A, const uint16_t* flags, size_t N, double* part, double* out,
+                                         cudaStream_t s);
 cudaError_t launch_macro_error(lbm_handle* h, lbm_handle* ref, double* d_out4, cudaStream_t s);
 cudaError_t launch_macro_rgba16f(lbm_handle* h, uint16_t* d_rgba, cudaStream_t s);
 cudaError_t launch_to_absolute(lbm_handle* h, const void* state, void* dst, int dst_dtype, cudaStream_t s);

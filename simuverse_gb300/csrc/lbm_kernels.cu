@@ -463,6 +463,8 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
             k_ref_step<false><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
         return cudaGetLastError();
     }
+    if (h->p.kernel == LBM_KERNEL_BULK || (h->p.kernel == LBM_KERNEL_AUTO && bulk_step_supported(h)))
+        return launch_phys_step_bulk(h, write_macro, s);
     if (h->p.kernel != LBM_KERNEL_CELL && vec_step_supported(h)) return launch_phys_step_vec(h, write_macro, s);
     switch (h->p.dtype) {
         case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
@@ -490,6 +492,13 @@ cudaError_t launch_conservation(lbm_handle* h, double* out, cudaStream_t s) {
         case LBM_DTYPE_F16: return conservation_t<StoreF16>(h, out, s);
         default: return conservation_t<StoreBF16>(h, out, s);
     }
+}
+
+cudaError_t launch_conservation_f32_phys(const float* A, const uint16_t* flags, size_t N, double* part, double* out,
+                                         cudaStream_t s) {
+    k_conservation<StoreF32, LBM_MODE_PHYSICS><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, flags, N, part);
+    k_final_sum<3><<<1, RED_TPB, 0, s>>>(part, RED_BLOCKS, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_count_nonfinite(lbm_handle* h, cudaStream_t s) {

@@ -1,85 +1,14 @@
-// lbm_step_vec.cu -- physics-mode step with four cells per thread.
-//
-// Each thread owns cells x0..x0+3 of one row (x0 a multiple of 4, so every population
-// plane is read and written with one aligned vector access per thread: 16 B for FP32,
-// 8 B for FP16/BF16, 2 x 16 B for FP64).  The pull of a direction with e_x = +1 needs
-// x0-1..x0+2: the thread's own vector shifted by one, the missing element coming from the
-// left neighbour lane by a warp shuffle (lane 0 loads it).  e_x = -1 is the mirror image.
-// Periodic wrap at x = 0 / nx-1 falls out of the halo loads.  Bounce-back and moving-wall
-// corrections read the cell's own opposite population with a scalar load (only cells next
-// to a solid take that path).  The collision is phys_collide of lbm_cell.cuh, shared with
-// the one-cell-per-thread kernel.  Requires nx % 4 == 0.
+// lbm_step_vec.cu -- physics-mode step with four cells per thread (phys_cells4_update of
+// lbm_cell4.cuh): one aligned vector load and store per population plane and thread,
+// warp shuffles for the +-x shifted directions.  Requires nx % 4 == 0.
 //
 // Algorithmic traffic per cell update: 9 loads + 9 stores of the stored type (72 B FP32,
 // 36 B FP16/BF16, 144 B FP64) plus the 2-byte flag word.
-#include "lbm_cell.cuh"
+#include "lbm_cell4.cuh"
 #include "lbm_common.cuh"
 #include "lbm_internal.h"
 
 namespace lbm {
-
-template <class ST>
-struct Vec4;
-
-template <>
-struct Vec4<StoreF32> {
-    __device__ __forceinline__ static void ld(const float* p, float (&r)[4]) {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(p));
-        r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
-    }
-    __device__ __forceinline__ static void st(float* p, const float (&r)[4]) {
-        *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
-    }
-};
-
-template <>
-struct Vec4<StoreF64> {
-    __device__ __forceinline__ static void ld(const double* p, double (&r)[4]) {
-        const double2 a = __ldg(reinterpret_cast<const double2*>(p));
-        const double2 b = __ldg(reinterpret_cast<const double2*>(p + 2));
-        r[0] = a.x; r[1] = a.y; r[2] = b.x; r[3] = b.y;
-    }
-    __device__ __forceinline__ static void st(double* p, const double (&r)[4]) {
-        reinterpret_cast<double2*>(p)[0] = make_double2(r[0], r[1]);
-        reinterpret_cast<double2*>(p)[1] = make_double2(r[2], r[3]);
-    }
-};
-
-template <>
-struct Vec4<StoreF16> {
-    __device__ __forceinline__ static void ld(const __half* p, float (&r)[4]) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
-        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
-        const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
-        r[0] = a.x * F16_INV_SCALE; r[1] = a.y * F16_INV_SCALE; r[2] = b.x * F16_INV_SCALE; r[3] = b.y * F16_INV_SCALE;
-    }
-    __device__ __forceinline__ static void st(__half* p, const float (&r)[4]) {
-        const __half2 a = __floats2half2_rn(r[0] * F16_SCALE, r[1] * F16_SCALE);
-        const __half2 b = __floats2half2_rn(r[2] * F16_SCALE, r[3] * F16_SCALE);
-        uint2 q;
-        q.x = *reinterpret_cast<const unsigned*>(&a);
-        q.y = *reinterpret_cast<const unsigned*>(&b);
-        *reinterpret_cast<uint2*>(p) = q;
-    }
-};
-
-template <>
-struct Vec4<StoreBF16> {
-    __device__ __forceinline__ static void ld(const __nv_bfloat16* p, float (&r)[4]) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
-        const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.x));
-        const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.y));
-        r[0] = a.x; r[1] = a.y; r[2] = b.x; r[3] = b.y;
-    }
-    __device__ __forceinline__ static void st(__nv_bfloat16* p, const float (&r)[4]) {
-        const __nv_bfloat162 a = __floats2bfloat162_rn(r[0], r[1]);
-        const __nv_bfloat162 b = __floats2bfloat162_rn(r[2], r[3]);
-        uint2 q;
-        q.x = *reinterpret_cast<const unsigned*>(&a);
-        q.y = *reinterpret_cast<const unsigned*>(&b);
-        *reinterpret_cast<uint2*>(p) = q;
-    }
-};
 
 constexpr int VEC_TPB = 128;  // 512 cells of a row per block
 
@@ -88,103 +17,8 @@ __global__ void __launch_bounds__(VEC_TPB) k_phys_step_v4(const typename ST::T* 
                                                           typename ST::T* __restrict__ B, uint16_t* __restrict__ flags,
                                                           lbm_lattice_info* __restrict__ info, typename ST::R omega,
                                                           int nx, int ny, float* __restrict__ macro) {
-    using R = typename ST::R;
-    using T = typename ST::T;
-    const int lane = threadIdx.x & 31;
     const int x0 = (blockIdx.x * VEC_TPB + threadIdx.x) * 4;
-    const int y = blockIdx.y;
-    const bool active = x0 < nx;
-    const size_t N = (size_t)nx * ny;
-    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
-    const int xl = x0 == 0 ? nx - 1 : x0 - 1;
-    const int xr = x0 + 4 >= nx ? 0 : x0 + 4;
-    const bool own_left = lane == 0;
-    const bool own_right = lane == 31 || x0 + 4 >= nx;
-
-    unsigned fl[4] = {LBM_BOUNDARY, LBM_BOUNDARY, LBM_BOUNDARY, LBM_BOUNDARY};
-    if (active) {
-        const uint2 q = *reinterpret_cast<const uint2*>(flags + r0 + x0);
-        fl[0] = q.x & 0xffffu; fl[1] = q.x >> 16; fl[2] = q.y & 0xffffu; fl[3] = q.y >> 16;
-    }
-
-    R d[9][4];
-    R al[3][4];  // unshifted vectors of the e_x = -1 planes (zero-gradient outflow)
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        const T* Aj = A + (size_t)j * N + row;
-        R v[4] = {R(0), R(0), R(0), R(0)};
-        if (active) Vec4<ST>::ld(Aj + x0, v);
-        if (EX(j) == 0) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) d[j][k] = v[k];
-        } else if (EX(j) == 1) {  // source x - 1
-            R prev = __shfl_up_sync(0xffffffffu, v[3], 1);
-            if (own_left && active) prev = ST::ld(Aj + xl);
-            d[j][0] = prev; d[j][1] = v[0]; d[j][2] = v[1]; d[j][3] = v[2];
-        } else {  // source x + 1
-            R next = __shfl_down_sync(0xffffffffu, v[0], 1);
-            if (own_right && active) next = ST::ld(Aj + xr);
-            d[j][0] = v[1]; d[j][1] = v[2]; d[j][2] = v[3]; d[j][3] = next;
-            const int a = j == 3 ? 0 : (j == 6 ? 1 : 2);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) al[a][k] = v[k];
-        }
-    }
-    if (!active) return;
-
-    R mr[4], mu[4], mv[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const unsigned f = fl[k];
-        const int m = (int)(f & FL_MAT_MASK);
-        const int x = x0 + k;
-        const size_t c = r0 + x;
-        R dk[9];
-#pragma unroll
-        for (int j = 0; j < 9; ++j) dk[j] = d[j][k];
-        if (is_solid(m)) {
-#pragma unroll
-            for (int j = 0; j < 9; ++j) d[j][k] = R(0);
-            mr[k] = R(0); mu[k] = R(0); mv[k] = R(0);
-            continue;
-        }
-        if (m == LBM_OUTLET) {  // zero-gradient: e_x = -1 populations come from the own column
-            dk[3] = al[0][k]; dk[6] = al[1][k]; dk[7] = al[2][k];
-        }
-        if (f & (0xFFu << (FL_DIR_SHIFT + 1))) {  // some pull source is solid: bounce back
-#pragma unroll
-            for (int j = 1; j < 9; ++j) {
-                if (f & (1u << (FL_DIR_SHIFT + j))) {
-                    R v = ST::ld(A + c + (size_t)INV(j) * N);
-                    if (f & FL_MOVING) {
-                        int sx = x - EX(j);
-                        if (m == LBM_OUTLET && EX(j) == -1) sx = x;
-                        sx = sx < 0 ? nx - 1 : (sx >= nx ? 0 : sx);
-                        const size_t srow = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-                        const lbm_lattice_info si = info[srow + sx];
-                        const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
-                        if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j), uw));
-                    }
-                    dk[j] = v;
-                }
-            }
-        }
-        R o[9];
-        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k]);
-#pragma unroll
-        for (int j = 0; j < 9; ++j) d[j][k] = o[j];
-    }
-#pragma unroll
-    for (int j = 0; j < 9; ++j) Vec4<ST>::st(B + (size_t)j * N + r0 + x0, d[j]);
-    if (MACRO) {
-        *reinterpret_cast<float4*>(macro + r0 + x0) = make_float4((float)mr[0], (float)mr[1], (float)mr[2], (float)mr[3]);
-        *reinterpret_cast<float4*>(macro + N + r0 + x0) =
-            make_float4((float)mu[0], (float)mu[1], (float)mu[2], (float)mu[3]);
-        *reinterpret_cast<float4*>(macro + 2 * N + r0 + x0) =
-            make_float4((float)mv[0], (float)mv[1], (float)mv[2], (float)mv[3]);
-    }
+    phys_cells4_update<ST, MACRO>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
 }
 
 template <class ST, bool MACRO>

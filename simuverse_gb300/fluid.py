@@ -191,6 +191,10 @@ class FluidSimulator:
             nat.check(rc)
         return int(n.value)
 
+    def status(self):
+        """Raises LbmError(LBM_ERR_TIMEOUT) if a step kernel gave up on a bounded wait."""
+        nat.check(self._lib.lbm_status(self._h))
+
     def check_finite(self):
         n = ctypes.c_uint64(0)
         nat.check(self._lib.lbm_check_finite(self._h, ctypes.byref(n)))
