@@ -201,6 +201,23 @@ int lbm_macro_error(lbm_handle* h, lbm_handle* ref, double out[4]);
 int lbm_save(lbm_handle* h, const char* path);
 int lbm_load(lbm_handle* h, const char* path);
 
+/* Allocation-free FP64 sums -- no counterpart in the reference.  The same three sums as
+   lbm_conservation (bit-identical for the same populations), computed over device
+   buffers the caller owns: d_populations in the storage format of (mode, dtype) -- 9
+   planes of nx*ny values, absolute f for reference mode, f - w (FP16: times 2^10) for
+   physics mode -- d_info (device, nx*ny records; needed in physics mode to skip solids),
+   d_out (device, 3 doubles).  For callers that cannot allocate device memory: a host
+   application whose own runtime owns every device buffer, a process whose device memory
+   is claimed by another allocator's pool, or a real-time loop that cannot afford
+   cudaMalloc's device synchronisation.  The library allocates nothing on this path: its
+   scratch is a fixed 29,184-byte array (1216 x 3 doubles) that every GPU loading the
+   library keeps until exit.  Limit: lattices up to 2^30 cells (larger ones are rejected
+   with LBM_ERR_ARG).  The first call on a device resolves the scratch address on that
+   device (make it before any stream capture).  Calls share the scratch: calls that overlap
+   on the GPU race.  Asynchronous on cuda_stream (NULL: the legacy default stream). */
+int lbm_conservation_noalloc(const void* d_populations, int32_t dtype, int32_t mode, const lbm_lattice_info* d_info,
+                             int32_t nx, int32_t ny, double* d_out, void* cuda_stream);
+
 /* synchronises; LBM_ERR_TIMEOUT if a step kernel gave up on a bounded wait since creation
    -- no counterpart in the reference */
 int lbm_status(lbm_handle* h);

@@ -102,6 +102,7 @@ _SIGNATURES = {
     "lbm_macro_error": [_P, _P, ctypes.POINTER(_D)],
     "lbm_save": [_P, ctypes.c_char_p],
     "lbm_load": [_P, ctypes.c_char_p],
+    "lbm_conservation_noalloc": [_P, _I, _I, _P, _I, _I, _P, _P],
     "lbm_status": [_P],
     "lbm_steps_done": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_kernel_launches": [_P, ctypes.POINTER(ctypes.c_uint64)],
