@@ -293,6 +293,91 @@ def run_gpu(args):
         pg.destroy_process_group()
 
 
+def run_precision(args):
+    """Precision form at 8192^2: GLUPS of FP32 / FP16 / BF16 storage with each kernel
+    variant, and the error of each against an FP64 run of the same channel after
+    args.steps steps (rel L2 of rho and u, FP64 mass drift)."""
+    import torch
+
+    from simuverse_gb300 import FluidSimulator
+
+    nx = ny = args.nx
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    out = {"workload": "precision", "nx": nx, "ny": ny, "glups": {}, "errors": {}}
+    base = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
+                seed=1234)
+    for dtype in ("f32", "f16", "bf16"):
+        for kernel in ("cell", "vec4", "bulk"):
+            sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel, **base)
+            sim.set_stream(stream.cuda_stream)
+            sim.step(args.warmup)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            sim.step(args.timing_steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            g = nx * ny * args.timing_steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+            out["glups"]["%s/%s" % (dtype, kernel)] = g
+            sim.close()
+    for tau in args.taus:
+        ref = FluidSimulator(nx, ny, dtype="f64", tau=tau, **base)
+        m0 = ref.conservation()[0]
+        ref.step(args.steps)
+        m_ref = ref.conservation()[0]
+        row = {"fp64_mass_drift": (m_ref - m0) / m0}
+        for dtype in ("f32", "f16", "bf16"):
+            sim = FluidSimulator(nx, ny, dtype=dtype, tau=tau, **base)
+            s0 = sim.conservation()[0]
+            sim.step(args.steps)
+            err = sim.macro_error(ref)
+            row[dtype] = {"rel_l2_rho": err[0], "rel_l2_u": err[1], "max_du": err[2],
+                          "mass_drift": (sim.conservation()[0] - s0) / s0, "nonfinite": sim.nonfinite_count()}
+            sim.close()
+        ref.close()
+        out["errors"]["tau=%g" % tau] = row
+    out["steps"] = args.steps
+    print(json.dumps(out), flush=True)
+
+
+def run_batch(args):
+    """Batched form: seeded list of 256 cavities and channels; aggregate GLUPS of the
+    persistent CUDA-graph launch (autotuned) against a per-domain launch loop."""
+    import torch
+
+    from simuverse_gb300 import BatchSimulator, generate_domains
+
+    doms = generate_domains(args.domains, args.seed)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    out = {"workload": "batch", "domains": len(doms)}
+    b = BatchSimulator(doms)
+    b.set_stream(stream.cuda_stream)
+    out["cells"] = b.cells
+    t0 = time.perf_counter()
+    out["tuned"] = b.tune(trial_steps=10)
+    out["tune_seconds"] = time.perf_counter() - t0
+    res = {}
+    for method, steps in (("persistent", args.steps), ("tile_launches", args.steps), ("domain_loop", args.loop_steps)):
+        b.configure(method=method)
+        b.step(3)
+        b.status()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        b.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        b.status()
+        ms = e0.elapsed_time(e1)
+        res[method] = {"steps": steps, "ms_per_step": ms / steps, "glups": b.cells * steps / (ms * 1e-3) / 1e9,
+                       "gb_per_s": 72 * b.cells * steps / (ms * 1e-3) / 1e9}
+    out["methods"] = res
+    out["persistent_over_loop"] = res["persistent"]["glups"] / res["domain_loop"]["glups"]
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -304,11 +389,21 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch"])
+    ap.add_argument("--taus", type=float, nargs="*", default=[0.51, 0.6, 0.9])
+    ap.add_argument("--timing-steps", type=int, default=500)
+    ap.add_argument("--domains", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--loop-steps", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "precision":
+        run_precision(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

@@ -254,12 +254,13 @@ typedef struct lbm_domain_desc {
 } lbm_domain_desc;
 
 typedef struct lbm_batch_config {
-    int32_t tile_threads_x; /* threads per tile row (multiple of 32); a tile is 4x that wide */
-    int32_t tile_rows;      /* rows per tile (threads per block = tile_threads_x * tile_rows <= 256) */
-    int32_t blocks_per_sm;  /* persistent grid = blocks_per_sm x SMs (0: occupancy maximum) */
-    int32_t method;         /* LBM_BATCH_* */
-    float ms_per_step;      /* filled by lbm_batch_tune */
-    int32_t reserved[3];
+    int32_t tile_threads_x;   /* threads per tile row (multiple of 32) */
+    int32_t tile_rows;        /* rows per tile (threads per block = tile_threads_x * tile_rows <= 256) */
+    int32_t blocks_per_sm;    /* persistent grid = blocks_per_sm x SMs (0: occupancy maximum) */
+    int32_t method;           /* LBM_BATCH_* */
+    float ms_per_step;        /* filled by lbm_batch_tune */
+    int32_t cells_per_thread; /* 1, or 4 (vector accesses); a tile is cells_per_thread * tile_threads_x wide */
+    int32_t reserved[2];
 } lbm_batch_config;
 
 typedef struct lbm_batch lbm_batch;

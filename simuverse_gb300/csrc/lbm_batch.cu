@@ -7,7 +7,8 @@
 // (planes of domain d at pop_off[d] + j * pitch * ny), flags / info / macro in pooled
 // arrays at cell_off[d].
 //
-// Work.  Domains are cut into tiles of (4 * tx) x ty cells; a tile list covers them all.
+// Work.  Domains are cut into tiles of (cells_per_thread * tx) x ty cells; a tile list
+// covers them all (one cell per thread, or four with vector accesses).
 // Method 0: one cooperative persistent launch runs every step: blocks take tiles
 // round-robin, then meet at a grid barrier before the next step.  The barrier spins with
 // a time limit: a block that waits longer sets an error word (LBM_ERR_TIMEOUT), every
@@ -95,6 +96,8 @@ __device__ bool grid_barrier(BarrierState* bar, unsigned target, unsigned long l
     return s_ok != 0;
 }
 
+// one tile = (cells_per_thread * blockDim.x) x blockDim.y cells of one domain
+template <int CPT>
 __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms, int4 tl, const float* __restrict__ A0,
                                             float* __restrict__ B0, uint16_t* __restrict__ flags,
                                             lbm_lattice_info* __restrict__ info, float* __restrict__ macro,
@@ -102,19 +105,31 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
     const BatchDomain dm = doms[tl.x];
     const int y = tl.z + (int)threadIdx.y;
     if (y >= dm.ny) return;  // warp-uniform: a warp spans one row
-    const int x0 = tl.y + (int)threadIdx.x * 4;
-    const bool active = x0 < dm.nx;
     const float* A = A0 + dm.pop_off;
     float* B = B0 + dm.pop_off;
-    if (write_macro)
-        phys_cells4_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
-                                           dm.pitch, dm.ny, active, macro + 3 * dm.cell_off);
-    else
-        phys_cells4_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
-                                            dm.pitch, dm.ny, active, macro + 3 * dm.cell_off);
+    if (CPT == 1) {
+        const int x = tl.y + (int)threadIdx.x;
+        if (x >= dm.nx) return;
+        if (write_macro)
+            phys_cell_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
+                                             dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+        else
+            phys_cell_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
+                                              dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+    } else {
+        const int x0 = tl.y + (int)threadIdx.x * 4;
+        const bool active = x0 < dm.nx;
+        if (write_macro)
+            phys_cells4_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
+                                               dm.pitch, dm.ny, active, macro + 3 * dm.cell_off);
+        else
+            phys_cells4_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
+                                                dm.pitch, dm.ny, active, macro + 3 * dm.cell_off);
+    }
 }
 
 // method 0: all steps in one cooperative launch
+template <int CPT>
 __global__ void __launch_bounds__(256) k_batch_persistent(const BatchDomain* __restrict__ doms,
                                                           const int4* __restrict__ tiles, int ntiles, float* pool0,
                                                           float* pool1, uint16_t* flags, lbm_lattice_info* info,
@@ -125,32 +140,35 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BatchDomain* __r
         const float* A = odd ? pool1 : pool0;
         float* B = odd ? pool0 : pool1;
         const bool mac = (s == nsteps - 1);
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) tile_update(doms, tiles[t], A, B, flags, info, macro, mac);
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+            tile_update<CPT>(doms, tiles[t], A, B, flags, info, macro, mac);
         if ((int)blockIdx.x == skip_block && s == skip_step) return;  // injected missing arrival (tests)
         if (!grid_barrier(bar, (unsigned)(s + 1) * gridDim.x, timeout_ns, s)) return;
     }
 }
 
 // method 1: one step over the tile list, one tile per block
+template <int CPT>
 __global__ void __launch_bounds__(256) k_batch_tiles(const BatchDomain* __restrict__ doms, const int4* __restrict__ tiles,
                                                      const float* A, float* B, uint16_t* flags, lbm_lattice_info* info,
                                                      float* macro, int write_macro) {
-    tile_update(doms, tiles[blockIdx.x], A, B, flags, info, macro, write_macro != 0);
+    tile_update<CPT>(doms, tiles[blockIdx.x], A, B, flags, info, macro, write_macro != 0);
 }
 
-// method 2: one domain per launch
-__global__ void __launch_bounds__(128) k_batch_domain(BatchDomain dm, const float* A0, float* B0, uint16_t* flags,
-                                                      lbm_lattice_info* info, float* macro, int write_macro) {
-    const int x0 = (blockIdx.x * 128 + threadIdx.x) * 4;
+// method 2: one domain per launch (the single-lattice one-cell kernel's layout)
+__global__ void __launch_bounds__(128, 16) k_batch_domain(BatchDomain dm, const float* A0, float* B0, uint16_t* flags,
+                                                          lbm_lattice_info* info, float* macro, int write_macro) {
+    const int x = blockIdx.x * 128 + threadIdx.x;
     const int y = blockIdx.y;
+    if (x >= dm.nx) return;
     const float* A = A0 + dm.pop_off;
     float* B = B0 + dm.pop_off;
     if (write_macro)
-        phys_cells4_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
-                                           dm.pitch, dm.ny, x0 < dm.nx, macro + 3 * dm.cell_off);
+        phys_cell_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx, dm.pitch,
+                                         dm.ny, macro + 3 * dm.cell_off);
     else
-        phys_cells4_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
-                                            dm.pitch, dm.ny, x0 < dm.nx, macro + 3 * dm.cell_off);
+        phys_cell_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
+                                          dm.pitch, dm.ny, macro + 3 * dm.cell_off);
 }
 
 // masks of the batch: cavity = solid ring with the row y = 0 moving at `speed`; channel =
@@ -286,7 +304,7 @@ void free_graph(lbm_batch* b) {
 }
 
 int build_tiles(lbm_batch* b) {
-    const int tw = 4 * b->cfg.tile_threads_x, th = b->cfg.tile_rows;
+    const int tw = b->cfg.cells_per_thread * b->cfg.tile_threads_x, th = b->cfg.tile_rows;
     std::vector<int4> tiles;
     for (size_t d = 0; d < b->doms.size(); ++d) {
         const lbm::BatchDomain& dm = b->doms[d];
@@ -306,7 +324,10 @@ int build_tiles(lbm_batch* b) {
 int persistent_grid(lbm_batch* b, int* grid) {
     int per_sm = 0;
     const int threads = b->cfg.tile_threads_x * b->cfg.tile_rows;
-    B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent, threads, 0));
+    if (b->cfg.cells_per_thread == 1)
+        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<1>, threads, 0));
+    else
+        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<4>, threads, 0));
     if (per_sm < 1) return bfail(LBM_ERR_ARG, "persistent kernel does not fit %d threads per block", threads);
     const int want = b->cfg.blocks_per_sm > 0 ? b->cfg.blocks_per_sm : per_sm;
     *grid = std::min(want, per_sm) * b->sms;
@@ -327,9 +348,14 @@ int launch_persistent(lbm_batch* b, int nsteps, int skip_block, int skip_step, c
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent, (const lbm::BatchDomain*)b->d_doms, (const int4*)b->d_tiles,
-                            b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info, b->d_macro, nsteps, b->cur,
-                            b->d_bar, b->timeout_ns, skip_block, skip_step));
+    if (b->cfg.cells_per_thread == 1)
+        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<1>, (const lbm::BatchDomain*)b->d_doms,
+                                (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
+                                b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
+    else
+        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<4>, (const lbm::BatchDomain*)b->d_doms,
+                                (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
+                                b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
     return LBM_OK;
 }
 
@@ -370,8 +396,12 @@ int run_steps(lbm_batch* b, int nsteps, int method) {
         for (int s = 0; s < nsteps; ++s) {
             const float* A = b->pool[(b->cur + s) & 1];
             float* B = b->pool[(b->cur + s + 1) & 1];
-            lbm::k_batch_tiles<<<(unsigned)b->ntiles, block, 0, b->stream>>>(b->d_doms, b->d_tiles, A, B, b->d_flags,
-                                                                             b->d_info, b->d_macro, s == nsteps - 1);
+            if (b->cfg.cells_per_thread == 1)
+                lbm::k_batch_tiles<1><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
+                    b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
+            else
+                lbm::k_batch_tiles<4><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
+                    b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
             B_CK(cudaGetLastError());
         }
         b->launches += nsteps;
@@ -380,7 +410,7 @@ int run_steps(lbm_batch* b, int nsteps, int method) {
             const float* A = b->pool[(b->cur + s) & 1];
             float* B = b->pool[(b->cur + s + 1) & 1];
             for (const lbm::BatchDomain& dm : b->doms) {
-                const dim3 grid((unsigned)((dm.pitch / 4 + 127) / 128), (unsigned)dm.ny);
+                const dim3 grid((unsigned)((dm.nx + 127) / 128), (unsigned)dm.ny);
                 lbm::k_batch_domain<<<grid, 128, 0, b->stream>>>(dm, A, B, b->d_flags, b->d_info, b->d_macro,
                                                                  s == nsteps - 1);
             }
@@ -476,8 +506,9 @@ int lbm_batch_create(int32_t n, const lbm_domain_desc* desc, lbm_batch** out) {
     b->cells = cells;
     b->live_cells = live;
     b->pop_elems = pop;
-    b->cfg.tile_threads_x = 64;
+    b->cfg.tile_threads_x = 128;
     b->cfg.tile_rows = 2;
+    b->cfg.cells_per_thread = 1;
     b->cfg.blocks_per_sm = 0;
     b->cfg.method = LBM_BATCH_PERSISTENT;
     b->cfg.ms_per_step = 0.0f;
@@ -558,8 +589,9 @@ int lbm_batch_set_config(lbm_batch* b, const lbm_batch_config* cfg) {
         return bfail(LBM_ERR_ARG, "tile of %d x %d threads: tx must be a multiple of 32 and tx*ty <= 256", tx, ty);
     if (cfg->blocks_per_sm < 0 || cfg->blocks_per_sm > 32) return bfail(LBM_ERR_ARG, "blocks_per_sm out of range");
     if (cfg->method < LBM_BATCH_PERSISTENT || cfg->method > LBM_BATCH_DOMAIN_LOOP) return bfail(LBM_ERR_ARG, "unknown method");
+    if (cfg->cells_per_thread != 1 && cfg->cells_per_thread != 4) return bfail(LBM_ERR_ARG, "cells_per_thread must be 1 or 4");
     B_CK(cudaStreamSynchronize(b->stream));
-    const bool retile = tx != b->cfg.tile_threads_x || ty != b->cfg.tile_rows;
+    const bool retile = tx != b->cfg.tile_threads_x || ty != b->cfg.tile_rows || cfg->cells_per_thread != b->cfg.cells_per_thread;
     b->cfg = *cfg;
     if (retile) B_TRY(build_tiles(b));
     free_graph(b);
@@ -610,20 +642,23 @@ int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best_out
         if (best_out) *best_out = it->second;
         return LBM_OK;
     }
-    const int txs[] = {32, 64, 128};
+    const int cpts[] = {1, 4};
+    const int txs[] = {32, 64, 128, 256};
     const int tys[] = {1, 2, 4};
-    const int bps[] = {0, 1, 2, 3, 4, 6, 8};
+    const int bps[] = {0, 2, 4, 6, 8, 12, 16};
     lbm_batch_config best = b->cfg;
     best.method = LBM_BATCH_PERSISTENT;
     float best_ms = 1e30f;
     cudaEvent_t e0, e1;
     B_CK(cudaEventCreate(&e0));
     B_CK(cudaEventCreate(&e1));
+    for (int cpt : cpts)
     for (int tx : txs)
         for (int ty : tys) {
             if (tx * ty > 256) continue;
             for (int bp : bps) {
                 lbm_batch_config c = b->cfg;
+                c.cells_per_thread = cpt;
                 c.tile_threads_x = tx;
                 c.tile_rows = ty;
                 c.blocks_per_sm = bp;

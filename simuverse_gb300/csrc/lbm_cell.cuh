@@ -111,14 +111,16 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
     uy_out = uy;
 }
 
+// One cell (x, y) of a lattice of nx x ny cells whose rows are `pitch` elements apart
+// (pitch >= nx; the single-lattice kernel passes pitch = nx).
 template <class ST, bool MACRO>
 __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
-                                                 typename ST::R omega, int x, int y, int nx, int ny,
+                                                 typename ST::R omega, int x, int y, int nx, int pitch, int ny,
                                                  float* __restrict__ macro) {
     using R = typename ST::R;
-    const size_t N = (size_t)nx * ny;
-    const unsigned c = (unsigned)y * (unsigned)nx + (unsigned)x;  // cells < 2^30
+    const size_t N = (size_t)pitch * ny;
+    const unsigned c = (unsigned)y * (unsigned)pitch + (unsigned)x;  // cells < 2^31
     const unsigned fl = flags[c];
     const int m = (int)(fl & FL_MAT_MASK);
     if (is_solid(m)) {
@@ -128,7 +130,7 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
     const bool outlet = (m == LBM_OUTLET);
     const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
     const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const unsigned r0 = (unsigned)y * nx, rm = (unsigned)ym * nx, rp = (unsigned)yp * nx;
+    const unsigned r0 = (unsigned)y * pitch, rm = (unsigned)ym * pitch, rp = (unsigned)yp * pitch;
     R d[9];
     if (!(fl & (0x1FEu << FL_DIR_SHIFT))) {  // no solid neighbour: plain pull
 #pragma unroll

@@ -227,13 +227,13 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
 // physics-mode step (cell update in lbm_cell.cuh)
 // ------------------------------------------------------------------------------------
 template <class ST, bool MACRO>
-__global__ void __launch_bounds__(TPB) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
+__global__ void __launch_bounds__(TPB, 16) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                    typename ST::R omega, int nx, int ny, float* __restrict__ macro) {
     const int x = blockIdx.x * TPB + threadIdx.x;
     const int y = blockIdx.y;
     if (x >= nx) return;
-    phys_cell_update<ST, MACRO>(A, B, flags, info, omega, x, y, nx, ny, macro);
+    phys_cell_update<ST, MACRO>(A, B, flags, info, omega, x, y, nx, nx, ny, macro);
 }
 
 // ------------------------------------------------------------------------------------
