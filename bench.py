@@ -308,7 +308,7 @@ def run_precision(args):
     base = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
                 seed=1234)
     for dtype in ("f32", "f16", "bf16"):
-        for kernel in ("cell", "vec4", "bulk"):
+        for kernel in ("cell", "vec2", "vec4", "bulk"):
             sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel, **base)
             sim.set_stream(stream.cuda_stream)
             sim.step(args.warmup)
@@ -388,7 +388,7 @@ def main():
     ap.add_argument("--ny", type=int, default=4096)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2"])
     ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch"])
     ap.add_argument("--taus", type=float, nargs="*", default=[0.51, 0.6, 0.9])
     ap.add_argument("--timing-steps", type=int, default=500)

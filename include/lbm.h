@@ -78,6 +78,16 @@ extern "C" {
 #define LBM_KERNEL_VEC4 2   /* four cells per thread, vector loads and stores (nx % 4 == 0) */
 #define LBM_KERNEL_BULK 3   /* four cells per thread fed by double-buffered bulk asynchronous
                                copies into shared memory, persistent blocks (nx % 8 == 0) */
+#define LBM_KERNEL_VEC2 4   /* two cells per thread, one 32-bit access per plane for 16-bit
+                               storage (nx % 2 == 0) */
+
+/* physics-mode collision */
+#define LBM_COLLISION_BGK 0          /* single relaxation time */
+#define LBM_COLLISION_REGULARIZED 1  /* BGK after projecting f_neq on the second-order Hermite
+                                        moments (same viscosity) */
+#define LBM_COLLISION_MRT 2          /* multiple relaxation times (Lallemand & Luo 2000 moments):
+                                        stresses at 1/tau, energy 1.1, energy square 1.0, energy
+                                        flux 1.2; stable much closer to tau = 1/2 than BGK */
 
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */
@@ -119,7 +129,8 @@ typedef struct lbm_params {
     int32_t macro_every_step;/* 1: write the macro field every step, as the reference does;
                                 0: only on the last step of each lbm_step call */
     int32_t kernel;          /* LBM_KERNEL_*: step kernel variant (results agree to rounding) */
-    int32_t reserved[5];
+    int32_t collision;       /* physics mode: LBM_COLLISION_BGK or LBM_COLLISION_REGULARIZED */
+    int32_t reserved[4];
 } lbm_params;
 
 typedef struct lbm_handle lbm_handle;

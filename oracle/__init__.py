@@ -34,8 +34,8 @@ def lib() -> ctypes.CDLL:
             "lo_add_obstacle": ([_I, _I, _P, _P, _I, _I], _I),
             "lo_on_click": ([_I, _I, _I, _P, _P, _F, _F], _I),
             "lo_add_external_force": ([_I, _I, _I, _P, _F, _F, _F, _F], None),
-            "lo_phys_step_f32": ([_I, _I, _F, _P, _P, _P, _P], None),
-            "lo_phys_step_f64": ([_I, _I, _D, _P, _P, _P, _P], None),
+            "lo_phys_step_f32": ([_I, _I, _F, _P, _P, _P, _P, _I], None),
+            "lo_phys_step_f64": ([_I, _I, _D, _P, _P, _P, _P, _I], None),
             "lo_phys_init_f32": ([_I, _I, _P, _P, _P, _P, _P], None),
             "lo_phys_init_f64": ([_I, _I, _P, _P, _P, _P, _P], None),
             "lo_mask_physics_cavity": ([_I, _I, _F, _P], None),
@@ -171,7 +171,8 @@ class PhysOracle:
 
     W = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
 
-    def __init__(self, info, tau, dtype=np.float32):
+    def __init__(self, info, tau, dtype=np.float32, collision=0):
+        self.collision = int(collision)
         self.info = np.ascontiguousarray(info, INFO_DTYPE).copy()
         self.ny, self.nx = self.info.shape
         self.dtype = np.dtype(dtype)
@@ -201,7 +202,7 @@ class PhysOracle:
         fn = getattr(lib(), "lo_phys_step_" + self._sfx())
         for _ in range(n):
             fn(self.nx, self.ny, self.omega, _p(self.info), _p(self.bufs[self.cur]), _p(self.bufs[self.cur ^ 1]),
-               _p(self.macro3))
+               _p(self.macro3), self.collision)
             self.cur ^= 1
 
     @property

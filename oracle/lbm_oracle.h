@@ -69,9 +69,9 @@ void lo_add_external_force(int nx, int ny, int pixel_size, lo_info* dev_info,
  * outflow on an east face; 6 Guo body force (vx,vy) with the reference's block_iter
  * countdown.  Periodic wrap on both axes where no boundary intervenes. */
 void lo_phys_step_f32(int nx, int ny, float omega, lo_info* info, const float* A, float* B,
-                      float* macro3 /* rho, ux, uy planes; may be NULL */);
+                      float* macro3 /* rho, ux, uy planes; may be NULL */, int collision /* 0 BGK, 1 regularised */);
 void lo_phys_step_f64(int nx, int ny, double omega, lo_info* info, const double* A, double* B,
-                      double* macro3);
+                      double* macro3, int collision);
 /* equilibrium initialisation from macro fields (NULL -> rho=1, u=0); solids get 0 */
 void lo_phys_init_f32(int nx, int ny, const lo_info* info, const float* rho, const float* ux,
                       const float* uy, float* A);

@@ -26,7 +26,8 @@ LBM_ERR_NOMEM = -7
 MODES = {"reference": 0, "physics": 1}
 DTYPES = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4}
-KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3}
+KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3, "vec2": 4}
+COLLISIONS = {"bgk": 0, "regularized": 1, "mrt": 2}
 BULK, BOUNDARY, INLET, OBSTACLE, OUTLET, EXTERNAL_FORCE, GHOST = 1, 2, 3, 4, 5, 6, 7
 
 # LatticeInfo (simuverse/src/fluid/lattice.rs:5-13)
@@ -41,7 +42,7 @@ class LbmParams(ctypes.Structure):
         ("solid_fraction", ctypes.c_float), ("disk_rmin", ctypes.c_float), ("disk_rmax", ctypes.c_float),
         ("seed", ctypes.c_uint64),
         ("pixel_size", ctypes.c_int32), ("macro_every_step", ctypes.c_int32),
-        ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
+        ("kernel", ctypes.c_int32), ("collision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
     ]
 
 
@@ -104,6 +105,21 @@ _SIGNATURES = {
     "lbm_save": [_P, ctypes.c_char_p],
     "lbm_load": [_P, ctypes.c_char_p],
     "lbm_conservation_noalloc": [_P, _I, _I, _P, _I, _I, _P, _P],
+    "lbm_closure_create": [_I, _I, ctypes.c_uint64, ctypes.POINTER(_P)],
+    "lbm_closure_destroy": [_P],
+    "lbm_closure_set_scales": [_P, _F, _F],
+    "lbm_closure_get_params": [_P, _P],
+    "lbm_closure_set_params": [_P, _P],
+    "lbm_coarsen": [_P, _P, _I, _F],
+    "lbm_closure_apply": [_P, _P],
+    "lbm_closure_reserve": [_P, _I, _I, _I],
+    "lbm_closure_add_pair": [_P, _P, _P, _I, _I],
+    "lbm_closure_pairs": [_P, ctypes.POINTER(_I)],
+    "lbm_closure_train": [_P, _I, _F, ctypes.c_uint64, ctypes.POINTER(_D)],
+    "lbm_closure_eval": [_P, _I, _I, ctypes.POINTER(_D)],
+    "lbm_closure_loss_grad": [_P, _I, _I, _P, _P, ctypes.POINTER(_D), _P],
+    "lbm_closure_predict": [_P, _P, _P],
+    "lbm_closure_counters": [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
     "lbm_status": [_P],
     "lbm_steps_done": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_kernel_launches": [_P, ctypes.POINTER(ctypes.c_uint64)],
@@ -141,6 +157,8 @@ def load() -> ctypes.CDLL:
     lib.lbm_abi_version.argtypes = []
     lib.lbm_last_error.restype = ctypes.c_char_p
     lib.lbm_last_error.argtypes = []
+    lib.lbm_closure_param_count.restype = ctypes.c_int
+    lib.lbm_closure_param_count.argtypes = []
     lib.lbm_params_default.restype = None
     lib.lbm_params_default.argtypes = [ctypes.POINTER(LbmParams)]
     for name, args in _SIGNATURES.items():
@@ -165,4 +183,4 @@ def ptr(a: np.ndarray) -> ctypes.c_void_p:
 
 def exported_symbols():
     """Names declared in include/lbm.h that the library must export."""
-    return ["lbm_abi_version", "lbm_last_error", "lbm_params_default"] + list(_SIGNATURES)
+    return ["lbm_abi_version", "lbm_last_error", "lbm_params_default", "lbm_closure_param_count"] + list(_SIGNATURES)

@@ -228,7 +228,13 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "scene %d exists in physics mode only", p.scene);
     if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
-    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_BULK) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_VEC2) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if (p.collision < LBM_COLLISION_BGK || p.collision > LBM_COLLISION_MRT)
+        return fail(LBM_ERR_ARG, "unknown collision %d", p.collision);
+    if (p.collision != LBM_COLLISION_BGK && p.mode != LBM_MODE_PHYSICS)
+        return fail(LBM_ERR_ARG, "reference mode is BGK only");
+    if (p.kernel == LBM_KERNEL_VEC2 && (p.mode != LBM_MODE_PHYSICS || p.nx % 2 != 0))
+        return fail(LBM_ERR_ARG, "the two-cell kernel needs physics mode and nx %% 2 == 0");
     if (p.kernel == LBM_KERNEL_VEC4 && (p.mode != LBM_MODE_PHYSICS || p.nx % 4 != 0))
         return fail(LBM_ERR_ARG, "the four-cell kernel needs physics mode and nx %% 4 == 0");
     if (p.kernel == LBM_KERNEL_BULK && (p.mode != LBM_MODE_PHYSICS || p.nx % 8 != 0))

@@ -13,13 +13,16 @@
 
 namespace lbm {
 
+// MRT relaxation rates of the non-hydrodynamic moments (energy, energy square, energy flux)
+constexpr double MRT_S_E = 1.1, MRT_S_EPS = 1.0, MRT_S_Q = 1.2;
+
 // Boundary rules on the pulled populations d (Zou-He inlet, anchored outflow), moments,
 // Guo forcing with countdown, BGK.  o receives the post-collision deviations; rho, ux, uy
 // the macroscopic values of the cell.
 template <class R>
 __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size_t c, uint16_t* __restrict__ flags,
                                              lbm_lattice_info* __restrict__ info, R omega, R (&o)[9], R& rho_out,
-                                             R& ux_out, R& uy_out) {
+                                             R& ux_out, R& uy_out, int collision = LBM_COLLISION_BGK) {
     const bool outlet = (m == LBM_OUTLET);
     if (m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
         const lbm_lattice_info in = info[c];
@@ -65,6 +68,74 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
     // w (drho + rho (4.5 (e.u)^2 - 1.5 u.u)) shared by the pair and an odd part 3 w rho e.u
     const R om = omega, om1 = R(1) - omega;
     const R r1 = rho * (R(3) * PW<R>(1)), r5 = rho * (R(3) * PW<R>(5));
+    if (collision == LBM_COLLISION_MRT) {
+        // multiple relaxation times on the orthogonal D2Q9 moments of Lallemand & Luo
+        // (2000): energy e, energy square eps, energy fluxes qx, qy relax at fixed rates,
+        // the stresses pxx, pxy at omega (same shear viscosity as BGK); density and
+        // momentum are untouched.  Moments of the deviations d; rest-state moments removed.
+        const R a = d[1] + d[3] + d[2] + d[4];    // axis populations
+        const R g = d[5] + d[6] + d[7] + d[8];    // diagonal populations
+        const R me = R(-4) * d[0] - a + R(2) * g;
+        const R meps = R(4) * d[0] - R(2) * a + g;
+        const R qx = R(-2) * (d[1] - d[3]) + ((d[5] - d[7]) + (d[8] - d[6]));
+        const R qy = R(-2) * (d[4] - d[2]) + ((d[7] - d[5]) + (d[8] - d[6]));
+        const R pxx = (d[1] + d[3]) - (d[2] + d[4]);
+        const R pxy = (d[8] + d[6]) - (d[5] + d[7]);
+        const R jxx = jx * ux, jyy = jy * uy;  // j^2 / rho split by component
+        const R eeq = R(-2) * drho + R(3) * (jxx + jyy);
+        const R epseq = drho - R(3) * (jxx + jyy);
+        const R de = R(MRT_S_E) * (eeq - me);       // delta m = -s (m - m_eq)
+        const R deps = R(MRT_S_EPS) * (epseq - meps);
+        const R dqx = R(MRT_S_Q) * (-jx - qx);
+        const R dqy = R(MRT_S_Q) * (-jy - qy);
+        const R dpxx = om * ((jxx - jyy) - pxx);
+        const R dpxy = om * (jx * uy - pxy);
+        // back to populations: f += M^T D^-1 delta m (row norms 36, 36, 12, 12, 4, 4)
+        const R ce = de * (R(1) / R(36)), cp = deps * (R(1) / R(36));
+        const R cqx = dqx * (R(1) / R(12)), cqy = dqy * (R(1) / R(12));
+        const R cxx = dpxx * R(0.25), cxy = dpxy * R(0.25);
+        const R axis = -ce - R(2) * cp;   // common part of the axis populations
+        const R diag = R(2) * ce + cp;    // common part of the diagonal populations
+        o[1] = d[1] + axis - R(2) * cqx + cxx;
+        o[3] = d[3] + axis + R(2) * cqx + cxx;
+        o[4] = d[4] + axis - R(2) * cqy - cxx;
+        o[2] = d[2] + axis + R(2) * cqy - cxx;
+        o[8] = d[8] + diag + cqx + cqy + cxy;
+        o[6] = d[6] + diag - cqx - cqy + cxy;
+        o[5] = d[5] + diag + cqx - cqy - cxy;
+        o[7] = d[7] + diag - cqx + cqy - cxy;
+    } else if (collision == LBM_COLLISION_REGULARIZED) {
+        // regularised BGK: the non-equilibrium part is replaced by its projection on the
+        // second-order Hermite moments before relaxation (same viscosity; the non-
+        // hydrodynamic moments are reset every step)
+        R q[9];
+        {
+            const R e1 = ux, e2 = uy, e3 = ux + uy, e4 = ux - uy;
+            const R s1 = PW<R>(1) * (drho + rho * (R(4.5) * e1 * e1 - usq)), a1 = r1 * e1;
+            const R s2 = PW<R>(1) * (drho + rho * (R(4.5) * e2 * e2 - usq)), a2 = r1 * e2;
+            const R s3 = PW<R>(5) * (drho + rho * (R(4.5) * e3 * e3 - usq)), a3 = r5 * e3;
+            const R s4 = PW<R>(5) * (drho + rho * (R(4.5) * e4 * e4 - usq)), a4 = r5 * e4;
+            q[1] = s1 + a1; q[3] = s1 - a1;
+            q[4] = s2 + a2; q[2] = s2 - a2;
+            q[8] = s3 + a3; q[6] = s3 - a3;
+            q[5] = s4 + a4; q[7] = s4 - a4;
+        }
+        R n[9];
+#pragma unroll
+        for (int j = 1; j < 9; ++j) n[j] = d[j] - q[j];
+        const R pd = (n[5] + n[6]) + (n[7] + n[8]);
+        const R pxx = (n[1] + n[3]) + pd, pyy = (n[2] + n[4]) + pd;
+        const R pxy = (n[8] + n[6]) - (n[5] + n[7]);
+        const R k1 = om1 * R(4.5) * PW<R>(1), k5 = om1 * R(4.5) * PW<R>(5);
+        const R third = R(1) / R(3);
+        const R ax = k1 * (R(2) * third * pxx - third * pyy);  // e = (+-1, 0)
+        const R ay = k1 * (R(2) * third * pyy - third * pxx);  // e = (0, +-1)
+        const R dg = k5 * (R(2) * third * (pxx + pyy));
+        o[1] = q[1] + ax; o[3] = q[3] + ax;
+        o[2] = q[2] + ay; o[4] = q[4] + ay;
+        o[8] = q[8] + (dg + k5 * R(2) * pxy); o[6] = q[6] + (dg + k5 * R(2) * pxy);
+        o[5] = q[5] + (dg - k5 * R(2) * pxy); o[7] = q[7] + (dg - k5 * R(2) * pxy);
+    } else {
     {  // 1 / 3: e = (+-1, 0)
         const R eu = ux;
         const R sym = om * (PW<R>(1) * (drho + rho * (R(4.5) * eu * eu - usq)));
@@ -93,6 +164,7 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
         o[5] = om1 * d[5] + (sym + asy);
         o[7] = om1 * d[7] + (sym - asy);
     }
+    }
     if (forced) {
         const R gf = R(1) - R(0.5) * omega;
         const R uF = ux * Fx + uy * Fy;
@@ -117,7 +189,7 @@ template <class ST, bool MACRO>
 __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                  typename ST::R omega, int x, int y, int nx, int pitch, int ny,
-                                                 float* __restrict__ macro) {
+                                                 float* __restrict__ macro, int collision = LBM_COLLISION_BGK) {
     using R = typename ST::R;
     const size_t N = (size_t)pitch * ny;
     const unsigned c = (unsigned)y * (unsigned)pitch + (unsigned)x;  // cells < 2^31
@@ -160,7 +232,7 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
         }
     }
     R o[9], rho, ux, uy;
-    phys_collide<R>(d, m, fl, c, flags, info, omega, o, rho, ux, uy);
+    phys_collide<R>(d, m, fl, c, flags, info, omega, o, rho, ux, uy, collision);
     if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
 #pragma unroll
     for (int j = 0; j < 9; ++j) ST::st(B + (size_t)j * N + c, o[j]);

@@ -1,9 +1,9 @@
-// lbm_cell4.cuh -- the physics-mode update of four consecutive cells of one row by one
-// thread, shared by the single-lattice kernel (lbm_step_vec.cu) and the batched persistent
+// lbm_cell4.cuh -- the physics-mode update of CPT (2 or 4) consecutive cells of one row by
+// one thread, shared by the single-lattice kernel (lbm_step_vec.cu) and the batched persistent
 // kernel (lbm_batch.cu).
 //
-// Cells x0..x0+3 (x0 a multiple of 4) of row y; rows are `pitch` elements apart
-// (pitch % 4 == 0, pitch >= nx) and cells x >= nx are padding, never read by a fluid
+// Cells x0..x0+CPT-1 (x0 a multiple of CPT) of row y; rows are `pitch` elements apart
+// (pitch % CPT == 0, pitch >= nx) and cells x >= nx are padding, never read by a fluid
 // cell.  Every population plane is read and written with one aligned vector access per
 // thread.  The pull of a direction with e_x = +1 needs x0-1..x0+2: the thread's own
 // vector shifted by one, the missing element coming from the left neighbour lane by a
@@ -83,11 +83,66 @@ struct Vec4<StoreBF16> {
     }
 };
 
-template <class ST, bool MACRO>
+template <class ST>
+struct Vec2;
+template <>
+struct Vec2<StoreF32> {
+    __device__ __forceinline__ static void ld(const float* p, float (&r)[2]) {
+        const float2 q = __ldg(reinterpret_cast<const float2*>(p));
+        r[0] = q.x; r[1] = q.y;
+    }
+    __device__ __forceinline__ static void st(float* p, const float (&r)[2]) {
+        *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
+    }
+};
+template <>
+struct Vec2<StoreF64> {
+    __device__ __forceinline__ static void ld(const double* p, double (&r)[2]) {
+        const double2 q = __ldg(reinterpret_cast<const double2*>(p));
+        r[0] = q.x; r[1] = q.y;
+    }
+    __device__ __forceinline__ static void st(double* p, const double (&r)[2]) {
+        *reinterpret_cast<double2*>(p) = make_double2(r[0], r[1]);
+    }
+};
+template <>
+struct Vec2<StoreF16> {
+    __device__ __forceinline__ static void ld(const __half* p, float (&r)[2]) {
+        const unsigned q = __ldg(reinterpret_cast<const unsigned*>(p));
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q));
+        r[0] = a.x * F16_INV_SCALE; r[1] = a.y * F16_INV_SCALE;
+    }
+    __device__ __forceinline__ static void st(__half* p, const float (&r)[2]) {
+        const __half2 a = __floats2half2_rn(r[0] * F16_SCALE, r[1] * F16_SCALE);
+        *reinterpret_cast<unsigned*>(p) = *reinterpret_cast<const unsigned*>(&a);
+    }
+};
+template <>
+struct Vec2<StoreBF16> {
+    __device__ __forceinline__ static void ld(const __nv_bfloat16* p, float (&r)[2]) {
+        const unsigned q = __ldg(reinterpret_cast<const unsigned*>(p));
+        const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q));
+        r[0] = a.x; r[1] = a.y;
+    }
+    __device__ __forceinline__ static void st(__nv_bfloat16* p, const float (&r)[2]) {
+        const __nv_bfloat162 a = __floats2bfloat162_rn(r[0], r[1]);
+        *reinterpret_cast<unsigned*>(p) = *reinterpret_cast<const unsigned*>(&a);
+    }
+};
+
+template <class ST, int CPT>
+struct VecN;
+template <class ST>
+struct VecN<ST, 4> : Vec4<ST> {};
+template <class ST>
+struct VecN<ST, 2> : Vec2<ST> {};
+
+template <class ST, bool MACRO, int CPT = 4>
 __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                    typename ST::R omega, int x0, int y, int nx, int pitch, int ny,
-                                                   bool active, float* __restrict__ macro) {
+                                                   bool active, float* __restrict__ macro,
+                                                   int collision = LBM_COLLISION_BGK) {
     using R = typename ST::R;
     using T = typename ST::T;
     const int lane = threadIdx.x & 31;
@@ -95,35 +150,48 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
     const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
     const size_t r0 = (size_t)y * pitch, rm = (size_t)ym * pitch, rp = (size_t)yp * pitch;
     const int xl = x0 == 0 ? nx - 1 : x0 - 1;
-    const int xr = x0 + 4 >= nx ? 0 : x0 + 4;
+    const int xr = x0 + CPT >= nx ? 0 : x0 + CPT;
     const bool own_left = lane == 0;
-    const bool own_right = lane == 31 || x0 + 4 >= nx;
+    const bool own_right = lane == 31 || x0 + CPT >= nx;
 
-    unsigned fl[4] = {LBM_BOUNDARY, LBM_BOUNDARY, LBM_BOUNDARY, LBM_BOUNDARY};
+    unsigned fl[CPT];
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) fl[k] = LBM_BOUNDARY;
     if (active) {
-        const uint2 q = *reinterpret_cast<const uint2*>(flags + r0 + x0);
-        fl[0] = q.x & 0xffffu; fl[1] = q.x >> 16; fl[2] = q.y & 0xffffu; fl[3] = q.y >> 16;
+        if (CPT == 4) {
+            const uint2 q = *reinterpret_cast<const uint2*>(flags + r0 + x0);
+            fl[0] = q.x & 0xffffu; fl[1] = q.x >> 16; fl[CPT > 2 ? 2 : 0] = q.y & 0xffffu; fl[CPT > 3 ? 3 : 0] = q.y >> 16;
+        } else {
+            const unsigned q = *reinterpret_cast<const unsigned*>(flags + r0 + x0);
+            fl[0] = q & 0xffffu; fl[1] = q >> 16;
+        }
     }
 
-    R d[9][4];
+    R d[9][CPT];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
         const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
         const T* Aj = A + (size_t)j * N + row;
-        R v[4] = {R(0), R(0), R(0), R(0)};
-        if (active) Vec4<ST>::ld(Aj + x0, v);
+        R v[CPT];
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) v[k] = R(0);
+        if (active) VecN<ST, CPT>::ld(Aj + x0, v);
         if (EX(j) == 0) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) d[j][k] = v[k];
+            for (int k = 0; k < CPT; ++k) d[j][k] = v[k];
         } else if (EX(j) == 1) {  // source x - 1
-            R prev = __shfl_up_sync(0xffffffffu, v[3], 1);
+            R prev = __shfl_up_sync(0xffffffffu, v[CPT - 1], 1);
             if (own_left && active) prev = ST::ld(Aj + xl);
-            d[j][0] = prev; d[j][1] = v[0]; d[j][2] = v[1]; d[j][3] = v[2];
+            d[j][0] = prev;
+#pragma unroll
+            for (int k = 1; k < CPT; ++k) d[j][k] = v[k - 1];
         } else {  // source x + 1
             R next = __shfl_down_sync(0xffffffffu, v[0], 1);
             if (own_right && active) next = ST::ld(Aj + xr);
-            d[j][0] = v[1]; d[j][1] = v[2]; d[j][2] = v[3]; d[j][3] = next;
-            if (x0 + 4 > nx && active) {  // row end inside this group: cell nx-1 wraps to 0
+#pragma unroll
+            for (int k = 0; k < CPT - 1; ++k) d[j][k] = v[k + 1];
+            d[j][CPT - 1] = next;
+            if (x0 + CPT > nx && active) {  // row end inside this group: cell nx-1 wraps to 0
                 const int k = nx - 1 - x0;
                 d[j][k < 0 ? 0 : k] = ST::ld(Aj);
             }
@@ -131,9 +199,9 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
     }
     if (!active) return;
 
-    R mr[4], mu[4], mv[4];
+    R mr[CPT], mu[CPT], mv[CPT];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < CPT; ++k) {
         const unsigned f = fl[k];
         const int m = (int)(f & FL_MAT_MASK);
         const int x = x0 + k;
@@ -171,18 +239,19 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             }
         }
         R o[9];
-        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k]);
+        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k], collision);
 #pragma unroll
         for (int j = 0; j < 9; ++j) d[j][k] = o[j];
     }
 #pragma unroll
-    for (int j = 0; j < 9; ++j) Vec4<ST>::st(B + (size_t)j * N + r0 + x0, d[j]);
+    for (int j = 0; j < 9; ++j) VecN<ST, CPT>::st(B + (size_t)j * N + r0 + x0, d[j]);
     if (MACRO) {
-        *reinterpret_cast<float4*>(macro + r0 + x0) = make_float4((float)mr[0], (float)mr[1], (float)mr[2], (float)mr[3]);
-        *reinterpret_cast<float4*>(macro + N + r0 + x0) =
-            make_float4((float)mu[0], (float)mu[1], (float)mu[2], (float)mu[3]);
-        *reinterpret_cast<float4*>(macro + 2 * N + r0 + x0) =
-            make_float4((float)mv[0], (float)mv[1], (float)mv[2], (float)mv[3]);
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            macro[r0 + x0 + k] = (float)mr[k];
+            macro[N + r0 + x0 + k] = (float)mu[k];
+            macro[2 * N + r0 + x0 + k] = (float)mv[k];
+        }
     }
 }
 

@@ -1,0 +1,236 @@
+// lbm_closure_kernels.cuh -- kernels of the learned closure for a coarsened lattice.
+//
+// Network: x0 (9 features, stored as 16 channels) -> conv3x3 16->32 + bias, ReLU -> x1
+//          -> conv3x3 32->32 + bias, ReLU -> x2 -> conv3x3 32->9 (stored as 16) + bias -> y.
+// Activations are BF16 in NHWC order ([image][row][column][channel]); accumulation is FP32.
+// The convolutions are implicit GEMMs on the tensor cores with mma.sync.m16n8k16 (BF16 in,
+// FP32 accumulate): a warp owns 16 consecutive cells of one row (GEMM rows) times all output
+// channels (GEMM columns); K runs over the 9 taps x input channels.  The block stages the 3
+// input rows it needs (64 + 2 cells each) and all weights in shared memory with a padded
+// per-cell stride of (C/2 + 4) words, which makes every fragment load bank-conflict free.
+//
+// Weight layout for the conv kernel: BF16 [tap][cout][cin] (cin contiguous), tap = 3 (dy+1) +
+// (dx+1).  The input-gradient pass of a layer is the same kernel run on the output gradient
+// with the taps flipped (tap -> 8 - tap) and the channel roles swapped.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "lbm_common.cuh"
+
+namespace lbm {
+namespace closure {
+
+constexpr int CONV_WARPS = 4;
+constexpr int CONV_CELLS = 16 * CONV_WARPS;  // cells of one row per block
+
+enum { EPI_BIAS_RELU = 0, EPI_BIAS_F32 = 1, EPI_MASK = 2 };
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                               unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const unsigned*>(&v);
+}
+
+template <int C>
+struct SmemStride {
+    static constexpr int WORDS = C / 2 + 4;  // 32-bit words per cell (padding breaks bank conflicts)
+};
+
+// One 3x3 convolution.  in: [nimg][H][W][CIN] bf16, out: [nimg][H][W][COUT] (bf16, or f32
+// for EPI_BIAS_F32), wk: [9][COUT][CIN] bf16, bias: [COUT] f32 (unused for EPI_MASK),
+// mask: [nimg][H][W][COUT] bf16 (EPI_MASK only: out = acc where mask > 0, else 0).
+// PERIODIC: coordinates wrap; otherwise cells outside the image read as zero.
+// Requires W % 16 == 0.  Grid: (ceil(W / 64), H, nimg), 128 threads.
+template <int CIN, int COUT, int EPI, bool PERIODIC>
+__global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16* __restrict__ in,
+                                                             void* __restrict__ out,
+                                                             const __nv_bfloat16* __restrict__ wk,
+                                                             const float* __restrict__ bias,
+                                                             const __nv_bfloat16* __restrict__ mask, int H, int W) {
+    constexpr int CS = SmemStride<CIN>::WORDS;
+    constexpr int ROWC = CONV_CELLS + 2;
+    constexpr int NT = COUT / 8;
+    extern __shared__ __align__(16) unsigned csm[];
+    unsigned* sin = csm;                     // [3][ROWC][CS]
+    unsigned* sw = csm + 3 * ROWC * CS;      // [9][COUT][CS]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int img = blockIdx.z, y = blockIdx.y, xs = blockIdx.x * CONV_CELLS;
+    const size_t img_off = (size_t)img * H * W;
+
+    // stage the input rows y-1..y+1, columns xs-1 .. xs+64 (16-byte vectors)
+    constexpr int VPC = CIN / 8;  // 16-byte vectors per cell
+    for (int i = tid; i < 3 * ROWC * VPC; i += 32 * CONV_WARPS) {
+        const int v = i % VPC, cell = (i / VPC) % ROWC, r = i / (VPC * ROWC);
+        int gy = y + r - 1, gx = xs + cell - 1;
+        uint4 val = make_uint4(0u, 0u, 0u, 0u);
+        bool ok = true;
+        if (PERIODIC) {
+            gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+            gx = gx < 0 ? gx + W : (gx >= W ? gx - W : gx);
+        } else {
+            ok = gy >= 0 && gy < H && gx >= 0 && gx < W;
+        }
+        if (ok) val = *reinterpret_cast<const uint4*>(in + (img_off + (size_t)gy * W + gx) * CIN + v * 8);
+        *reinterpret_cast<uint4*>(sin + (r * ROWC + cell) * CS + v * 4) = val;
+    }
+    // stage the weights
+    for (int i = tid; i < 9 * COUT * VPC; i += 32 * CONV_WARPS) {
+        const int v = i % VPC, row = i / VPC;  // row = tap * COUT + co
+        *reinterpret_cast<uint4*>(sw + row * CS + v * 4) = *reinterpret_cast<const uint4*>(wk + (size_t)row * CIN + v * 8);
+    }
+    __syncthreads();
+
+    const int x0 = xs + warp * 16;
+    if (x0 >= W) return;
+    const int g = lane >> 2, c = lane & 3;
+    float acc[NT][4];
+#pragma unroll
+    for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap % 3;  // smem row / column offsets (0..2)
+        const unsigned* ra = sin + (dy * ROWC + warp * 16 + g + dx) * CS;
+        const unsigned* rb = ra + 8 * CS;
+#pragma unroll
+        for (int kc = 0; kc < CIN / 16; ++kc) {
+            const unsigned a0 = ra[kc * 8 + c], a1 = rb[kc * 8 + c];
+            const unsigned a2 = ra[kc * 8 + c + 4], a3 = rb[kc * 8 + c + 4];
+#pragma unroll
+            for (int n = 0; n < NT; ++n) {
+                const unsigned* wb = sw + (tap * COUT + n * 8 + g) * CS + kc * 8 + c;
+                mma_bf16_16816(acc[n], a0, a1, a2, a3, wb[0], wb[4]);
+            }
+        }
+    }
+    // epilogue: thread holds rows g, g+8 (cells x0+g, x0+g+8) and columns n*8 + 2c, +1
+    const size_t cell0 = img_off + (size_t)y * W + x0 + g;
+#pragma unroll
+    for (int n = 0; n < NT; ++n) {
+        const int ch = n * 8 + 2 * c;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const size_t cell = cell0 + 8 * h;
+            float v0 = acc[n][2 * h], v1 = acc[n][2 * h + 1];
+            if (EPI == EPI_BIAS_RELU) {
+                v0 = fmaxf(v0 + bias[ch], 0.0f);
+                v1 = fmaxf(v1 + bias[ch + 1], 0.0f);
+                reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+            } else if (EPI == EPI_BIAS_F32) {
+                *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + cell * COUT + ch) =
+                    make_float2(v0 + bias[ch], v1 + bias[ch + 1]);
+            } else {
+                const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask + cell * COUT + ch);
+                v0 = __bfloat162float(mk.x) > 0.0f ? v0 : 0.0f;
+                v1 = __bfloat162float(mk.y) > 0.0f ? v1 : 0.0f;
+                reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+            }
+        }
+    }
+}
+
+template <int CIN, int COUT>
+constexpr size_t conv_smem_bytes() {
+    return (size_t)(3 * (CONV_CELLS + 2) + 9 * COUT) * SmemStride<CIN>::WORDS * 4;
+}
+
+// Weight gradients of one layer, FP32 on the CUDA cores:
+//   dW[tap][ci][co] = sum_cells x[cell + off(tap)][ci] * g[cell][co],  db[co] = sum_cells g[cell][co]
+// over the cells of rows [r0, r1) and columns [c0, c1) of every image (the region the loss
+// covers; inputs outside the image read as zero, or wrap when PERIODIC).  Each thread owns a
+// 4 (ci) x 8 (co) block of one tap.  Blocks loop over 64-cell row segments and write one
+// partial each; k_dweight_final sums the partials in a fixed order (deterministic).
+// blockDim = 9 * (CIN / 4) * (COUT / 8).  GT: gradient element type (bf16 or f32).
+template <int CIN, int COUT, class GT, bool PERIODIC>
+__global__ void k_dweight(const __nv_bfloat16* __restrict__ x, const GT* __restrict__ gr, int nimg, int H, int W,
+                          int r0, int r1, int c0, int c1, float* __restrict__ partials) {
+    constexpr int SEG = 64;
+    constexpr int CB = CIN / 4, OB = COUT / 8;
+    __shared__ float sx[3][SEG + 2][CIN + 1];
+    __shared__ float sg[SEG][COUT + 1];
+    const int tid = threadIdx.x;
+    const int tap = tid / (CB * OB), cb = (tid / OB) % CB, ob = tid % OB;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    float acc[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    float bacc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) bacc[j] = 0.0f;
+    const int segs_per_row = (c1 - c0 + SEG - 1) / SEG;
+    const long nseg = (long)nimg * (r1 - r0) * segs_per_row;
+    for (long s = blockIdx.x; s < nseg; s += gridDim.x) {
+        const int img = (int)(s / ((long)(r1 - r0) * segs_per_row));
+        const int rem = (int)(s % ((long)(r1 - r0) * segs_per_row));
+        const int y = r0 + rem / segs_per_row;
+        const int xs = c0 + (rem % segs_per_row) * SEG;
+        const int n = min(SEG, c1 - xs);
+        __syncthreads();
+        for (int i = tid; i < 3 * (SEG + 2) * CIN; i += blockDim.x) {
+            const int ci = i % CIN, cell = (i / CIN) % (SEG + 2), r = i / (CIN * (SEG + 2));
+            int gy = y + r - 1, gx = xs + cell - 1;
+            float v = 0.0f;
+            if (PERIODIC) {
+                gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+                gx = gx < 0 ? gx + W : (gx >= W ? gx - W : gx);
+                v = __bfloat162float(x[(((size_t)img * H + gy) * W + gx) * CIN + ci]);
+            } else if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+                v = __bfloat162float(x[(((size_t)img * H + gy) * W + gx) * CIN + ci]);
+            }
+            sx[r][cell][ci] = v;
+        }
+        for (int i = tid; i < SEG * COUT; i += blockDim.x) {
+            const int co = i % COUT, cell = i / COUT;
+            float v = 0.0f;
+            if (cell < n) v = static_cast<float>(gr[(((size_t)img * H + y) * W + xs + cell) * COUT + co]);
+            sg[cell][co] = v;
+        }
+        __syncthreads();
+        for (int cell = 0; cell < n; ++cell) {
+            float xv[4], gv[8];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) xv[i] = sx[dy + 1][cell + dx + 1][cb * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) gv[j] = sg[cell][ob * 8 + j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(xv[i], gv[j], acc[i][j]);
+            if (tap == 4 && cb == 0)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) bacc[j] += gv[j];
+        }
+    }
+    float* p = partials + (size_t)blockIdx.x * (9 * CIN * COUT + COUT);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) p[(tap * CIN + cb * 4 + i) * COUT + ob * 8 + j] = acc[i][j];
+    if (tap == 4 && cb == 0)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) p[9 * CIN * COUT + ob * 8 + j] = bacc[j];
+}
+
+// out[k] = scale * sum_b partials[b][k] in block order (deterministic)
+__global__ void k_dweight_final(const float* __restrict__ partials, int nblocks, int len, float scale,
+                                float* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += (double)partials[(size_t)b * len + k];
+    out[k] = (float)(s * (double)scale);
+}
+
+}  // namespace closure
+}  // namespace lbm

@@ -56,6 +56,7 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s);
 // four-cells-per-thread physics step (lbm_step_vec.cu)
 bool vec_step_supported(const lbm_handle* h);
 cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s);
+cudaError_t launch_phys_step_vec2(lbm_handle* h, bool write_macro, cudaStream_t s);
 // bulk-copy fed physics step (lbm_step_bulk.cu)
 bool bulk_step_supported(const lbm_handle* h);
 cudaError_t launch_phys_step_bulk(lbm_handle* h, bool write_macro, cudaStream_t s);

@@ -229,11 +229,12 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
 template <class ST, bool MACRO>
 __global__ void __launch_bounds__(TPB, 16) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
-                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro) {
+                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro,
+                                                   int collision) {
     const int x = blockIdx.x * TPB + threadIdx.x;
     const int y = blockIdx.y;
     if (x >= nx) return;
-    phys_cell_update<ST, MACRO>(A, B, flags, info, omega, x, y, nx, nx, ny, macro);
+    phys_cell_update<ST, MACRO>(A, B, flags, info, omega, x, y, nx, nx, ny, macro, collision);
 }
 
 // ------------------------------------------------------------------------------------
@@ -449,7 +450,7 @@ static cudaError_t phys_step_t(lbm_handle* h, cudaStream_t s) {
     using R = typename ST::R;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     k_phys_step<ST, MACRO><<<cell_grid(h), TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, omega, h->nx, h->ny, h->d_macro);
+                                                        h->d_info, omega, h->nx, h->ny, h->d_macro, h->p.collision);
     return cudaGetLastError();
 }
 
@@ -467,6 +468,7 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     // copy bandwidth at 4096^2 against 70.9 % for VEC4 and 68.6 % for BULK)
     if (h->p.kernel == LBM_KERNEL_BULK) return launch_phys_step_bulk(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
+    if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);
     switch (h->p.dtype) {
         case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
         case LBM_DTYPE_F64: return write_macro ? phys_step_t<StoreF64, true>(h, s) : phys_step_t<StoreF64, false>(h, s);

@@ -32,6 +32,25 @@ def random_velocity(n: int, seed: int, k0: float = 8.0, u_rms: float = 0.04, ny:
     return ux * s, uy * s
 
 
+def pressure_density(ux: np.ndarray, uy: np.ndarray, rho0: float = 1.0, cs2: float = 1.0 / 3.0):
+    """Density consistent with an incompressible velocity field: the pressure solves
+    lap p = -d_i u_j d_j u_i (periodic, spectral), and rho = rho0 (1 + p / cs2)."""
+    ny, nx = ux.shape
+    kx = 2j * np.pi * np.fft.fftfreq(nx)
+    ky = 2j * np.pi * np.fft.fftfreq(ny)
+    KX, KY = np.meshgrid(kx, ky)
+    U, V = np.fft.fft2(ux), np.fft.fft2(uy)
+    ux_x, ux_y = np.real(np.fft.ifft2(KX * U)), np.real(np.fft.ifft2(KY * U))
+    uy_x, uy_y = np.real(np.fft.ifft2(KX * V)), np.real(np.fft.ifft2(KY * V))
+    src = -(ux_x * ux_x + 2.0 * ux_y * uy_x + uy_y * uy_y)
+    k2 = -(KX * KX + KY * KY).real
+    k2[0, 0] = 1.0
+    ph = -np.fft.fft2(src) / k2
+    ph[0, 0] = 0.0
+    p = np.real(np.fft.ifft2(ph))
+    return rho0 * (1.0 + p / cs2)
+
+
 def coarse_grain(field: np.ndarray, factor: int) -> np.ndarray:
     """Block average of a (ny, nx) field over factor x factor blocks."""
     ny, nx = field.shape

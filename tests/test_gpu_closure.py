@@ -1,0 +1,135 @@
+"""Learned closure: the tensor-core convolutions against an FP64 restatement, gradients
+against the FP64 restatement, exact conservation of the projected correction, the
+coarse-graining operator, and training on the GPU reducing the loss."""
+import numpy as np
+import pytest
+
+from oracle import closure_ref as ref
+from simuverse_gb300 import FluidSimulator
+from simuverse_gb300.closure import Closure, coarsen
+from simuverse_gb300.turbulence import random_velocity
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_params(c, rng, scale=1.0):
+    W1, b1, W2, b2, W3, b3 = ref.unpack(c.params)
+    W1 = rng.standard_normal(W1.shape) * np.sqrt(2 / 81) * scale
+    W2 = rng.standard_normal(W2.shape) * np.sqrt(2 / 288) * scale
+    W3 = rng.standard_normal(W3.shape) * np.sqrt(1 / 288) * scale
+    b1 = 0.1 * rng.standard_normal(32)
+    b2 = 0.1 * rng.standard_normal(32)
+    b3 = 0.01 * rng.standard_normal(9)
+    return ref.pack(W1, b1, W2, b2, W3, b3)
+
+
+def _turbulent_sim(nx, ny, seed, tau=0.55, steps=20):
+    s = FluidSimulator(nx, ny, mode="physics", scene="periodic", tau=tau)
+    ux, uy = random_velocity(nx, seed, 2.0, 0.04, ny=ny)
+    s.init_equilibrium(None, ux.astype(np.float32), uy.astype(np.float32))
+    s.step(steps)
+    return s
+
+
+def test_forward_matches_fp64_restatement(gpu):
+    nx, ny = 64, 48
+    rng = np.random.default_rng(0)
+    c = Closure(nx, ny, seed=1, s_in=3000.0, s_out=500.0)
+    p = _random_params(c, rng)
+    c.params = p
+    sim = _turbulent_sim(nx, ny, 4)
+    delta = c.predict(sim)
+    # features from the state: s_in * f_neq
+    f = sim.read_populations(np.float64).transpose(1, 2, 0)  # (ny, nx, 9)
+    rho = f.sum(-1, keepdims=True)
+    ux = (f * ref.EX).sum(-1, keepdims=True) / rho
+    uy = (f * ref.EY).sum(-1, keepdims=True) / rho
+    eu = ref.EX * ux + ref.EY * uy
+    feq = ref.W9 * rho * (1 + 3 * eu + 4.5 * eu * eu - 1.5 * (ux * ux + uy * uy))
+    x0 = (3000.0 * (f - feq))[None]
+    _, _, _, y = ref.forward(x0, c.params, periodic=True, emulate_bf16=True)
+    expect = (ref.project(y) / 500.0)[0].transpose(2, 0, 1)
+    err = np.max(np.abs(delta - expect)) / np.max(np.abs(expect))
+    assert err < 2e-2, err
+    # the correction conserves density and momentum cell by cell
+    assert np.max(np.abs(delta.sum(0))) < 1e-6 * np.max(np.abs(delta)) + 1e-12
+    assert np.max(np.abs((delta * ref.EX[:, None, None]).sum(0))) < 1e-6 * np.max(np.abs(delta)) + 1e-12
+
+
+def test_gradients_match_fp64_restatement(gpu):
+    rng = np.random.default_rng(1)
+    c = Closure(64, 64, seed=2)
+    c.params = _random_params(c, rng)
+    c.reserve(4, 32, 2)
+    feats = rng.standard_normal((2, 32, 32, 9))
+    targets = 0.3 * rng.standard_normal((2, 32, 32, 9))
+    loss, g = c.loss_grad(feats, targets)
+    loss_ref, g_ref = ref.loss_and_grad(feats, targets, c.params, emulate_bf16=True)
+    assert abs(loss - loss_ref) / loss_ref < 1e-2
+    # per layer: relative L2 error and direction of the gradient
+    off = 0
+    for n in (9 * 9 * 32, 32, 9 * 32 * 32, 32, 9 * 32 * 9, 9):
+        a, b = g[off:off + n].astype(np.float64), g_ref[off:off + n]
+        off += n
+        rel = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
+        assert rel < 5e-2 and cos > 0.998, (n, rel, cos)
+
+
+def test_apply_conserves_mass_and_momentum(gpu):
+    nx, ny = 128, 64
+    rng = np.random.default_rng(3)
+    c = Closure(nx, ny, seed=3, s_in=3000.0, s_out=200.0)
+    c.params = _random_params(c, rng)
+    sim = _turbulent_sim(nx, ny, 5)
+    before = np.array(sim.conservation())
+    delta = c.predict(sim)
+    assert np.max(np.abs(delta)) > 1e-6  # a real correction
+    c.apply(sim)
+    after = np.array(sim.conservation())
+    assert abs(after[0] - before[0]) / before[0] < 1e-9
+    assert np.max(np.abs(after[1:] - before[1:])) < 1e-9 * before[0]
+
+
+def test_coarsen_conserves_block_sums(gpu):
+    F = 4
+    fine = _turbulent_sim(256, 128, 6, steps=10)
+    coarse = FluidSimulator(64, 32, mode="physics", scene="periodic", tau=0.5125)
+    coarsen(fine, coarse, F, 4.0)
+    mf, jxf, jyf = fine.conservation()
+    mc, jxc, jyc = coarse.conservation()
+    assert abs(mc - mf / F**2) / mc < 1e-6
+    assert abs(jxc - jxf / F**2) < 1e-6 * mc and abs(jyc - jyf / F**2) < 1e-6 * mc
+    # coarse velocity equals the block-averaged momentum over the block-averaged density
+    r, ux, uy = fine.read_macro()
+    fine.step(0)
+    rc, uxc, uyc = coarse.read_macro()
+    f = coarse.read_populations(np.float64)
+    rho_c = f.sum(0)
+    jx_c = (f * ref.EX[:, None, None]).sum(0)
+    ff = fine.read_populations(np.float64)
+    rb = ff.sum(0).reshape(32, F, 64, F).mean(axis=(1, 3))
+    jb = (ff * ref.EX[:, None, None]).sum(0).reshape(32, F, 64, F).mean(axis=(1, 3))
+    assert np.max(np.abs(rho_c - rb)) < 1e-6 and np.max(np.abs(jx_c - jb)) < 1e-6
+
+
+def test_training_reduces_the_loss(gpu):
+    nx = ny = 128
+    F = 4
+    c = Closure(nx, ny, seed=7, s_in=3000.0, s_out=3000.0)
+    c.reserve(24, 64, 4)
+    fine = _turbulent_sim(nx * F, ny * F, 11, tau=0.51, steps=0)
+    pred = FluidSimulator(nx, ny, mode="physics", scene="periodic", tau=0.5025)
+    target = FluidSimulator(nx, ny, mode="physics", scene="periodic", tau=0.5025)
+    rng = np.random.default_rng(0)
+    for k in range(24):
+        coarsen(fine, pred, F, 4.0)
+        pred.step(2)
+        fine.step(2 * F)
+        coarsen(fine, target, F, 4.0)
+        c.add_pair(pred, target, int(rng.integers(0, nx)), int(rng.integers(0, ny)))
+    assert c.npairs == 24
+    l0 = c.eval(0, 24)
+    c.train(300, lr=2e-3, seed=1)
+    l1 = c.eval(0, 24)
+    assert l1 < 0.8 * l0, (l0, l1)

@@ -133,11 +133,12 @@ def test_init_equilibrium_roundtrip(gpu):
 @pytest.mark.parametrize("scene,nx,ny", [("channel", 388, 150), ("cavity", 132, 100), ("periodic", 68, 36),
                                          ("channel", 1024, 96)])
 @pytest.mark.parametrize("dtype", ["f32", "f64", "f16", "bf16"])
-def test_vec4_kernel_matches_cell_kernel(gpu, scene, nx, ny, dtype):
-    """The four-cells-per-thread kernel agrees with the one-cell kernel (same arithmetic)."""
+@pytest.mark.parametrize("kernel", ["vec4", "vec2"])
+def test_vec_kernels_match_cell_kernel(gpu, scene, nx, ny, dtype, kernel):
+    """The two- and four-cells-per-thread kernels agree with the one-cell kernel."""
     kw = dict(mode="physics", dtype=dtype, scene=scene, tau=0.58, lid_speed=0.1, inlet_speed=0.05, seed=5,
               disk_radius=(4.0, 9.0))
-    a = FluidSimulator(nx, ny, kernel="vec4", **kw)
+    a = FluidSimulator(nx, ny, kernel=kernel, **kw)
     b = FluidSimulator(nx, ny, kernel="cell", **kw)
     if scene == "periodic":
         rng = np.random.default_rng(2)
@@ -196,3 +197,22 @@ def test_bulk_kernel_matches_cell_kernel(gpu, scene, nx, ny, dtype):
     assert np.max(np.abs(fa - fb)[:, fluid]) <= tol
     for x, y in zip(a.read_macro(), b.read_macro()):
         assert np.max(np.abs(x - y)[fluid]) <= 10 * tol
+
+
+@pytest.mark.parametrize("collision", ["regularized", "mrt"])
+def test_collision_variants_match_oracle(gpu, collision):
+    nx, ny = 96, 80
+    code = {"regularized": 1, "mrt": 2}[collision]
+    sim = FluidSimulator(nx, ny, mode="physics", scene="cavity", tau=0.55, lid_speed=0.08, collision=collision)
+    ref = oracle.PhysOracle(oracle.mask_physics_cavity(nx, ny, 0.08), 0.55, np.float32, collision=code)
+    sim.step(1)
+    ref.step(1)
+    e_rho, e_u = _macro_err(sim, ref, 0.08)
+    assert e_rho <= 1e-5 and e_u <= 1e-5
+    m0 = sim.conservation()[0]
+    sim.step(499)
+    ref.step(499)
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= 1e-4
+    assert abs(sim.conservation()[0] - m0) / m0 <= 1e-10

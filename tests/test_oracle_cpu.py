@@ -107,3 +107,31 @@ def test_channel_mask_properties():
     assert 0.05 <= frac < 0.06
     assert (a["material"][:, 0] == 3)[1:-1].all() and (a["material"][:, -1] == 5)[1:-1].all()
     assert (a["material"][0] == 2).all() and (a["material"][-1] == 2).all()
+
+
+def test_closure_oracle_backprop_matches_finite_differences():
+    from oracle import closure_ref as ref
+
+    rng = np.random.default_rng(0)
+    n = 9 * 9 * 32 + 32 + 9 * 32 * 32 + 32 + 9 * 32 * 9 + 9
+    p = rng.standard_normal(n) * 0.1
+    x0 = rng.standard_normal((1, 12, 12, 9))
+    T = 0.3 * rng.standard_normal((1, 12, 12, 9))
+    _, g = ref.loss_and_grad(x0, T, p, emulate_bf16=False)
+    for i in rng.choice(n, 12, replace=False):
+        e = np.zeros(n)
+        e[i] = 1e-6
+        fd = (ref.loss_and_grad(x0, T, p + e, False)[0] - ref.loss_and_grad(x0, T, p - e, False)[0]) / 2e-6
+        assert abs(fd - g[i]) <= 1e-5 * (abs(fd) + abs(g[i])) + 1e-12
+
+
+def test_closure_projection_conserves_moments():
+    from oracle import closure_ref as ref
+
+    v = np.random.default_rng(1).standard_normal((50, 9))
+    pv = ref.project(v)
+    assert np.max(np.abs(pv.sum(-1))) < 1e-12
+    assert np.max(np.abs((pv * ref.EX).sum(-1))) < 1e-12 and np.max(np.abs((pv * ref.EY).sum(-1))) < 1e-12
+    # the transpose really is the adjoint
+    g = np.random.default_rng(2).standard_normal((50, 9))
+    assert abs((ref.project(v) * g).sum() - (v * ref.project_t(g)).sum()) < 1e-10
