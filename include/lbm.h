@@ -87,7 +87,10 @@ extern "C" {
                                         moments (same viscosity) */
 #define LBM_COLLISION_MRT 2          /* multiple relaxation times (Lallemand & Luo 2000 moments):
                                         stresses at 1/tau, energy 1.1, energy square 1.0, energy
-                                        flux 1.2; stable much closer to tau = 1/2 than BGK */
+                                        flux 1.2 */
+#define LBM_COLLISION_KBC 3          /* entropic KBC: shear part at 1/tau (BGK's viscosity), higher
+                                        moments at a per-cell entropic rate; stable for under-
+                                        resolved turbulence near tau = 1/2 */
 
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */

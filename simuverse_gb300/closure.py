@@ -100,3 +100,173 @@ class Closure:
         nat.check(self._lib.lbm_closure_loss_grad(self._h, n, S, nat.ptr(feats), nat.ptr(targets), ctypes.byref(loss),
                                                   nat.ptr(g)))
         return float(loss.value), g
+
+
+# ---------------------------------------------------------------------------------------
+# periodic decaying turbulence: data, training and evaluation of the closure
+# ---------------------------------------------------------------------------------------
+class TurbulenceSetup:
+    """Fine lattice nf x nf with tau_f; coarse lattice nf/factor with the acoustically
+    scaled viscosity (tau_c - 1/2 = (tau_f - 1/2) / factor); the closure acts every
+    k_coarse coarse steps."""
+
+    def __init__(self, nf=4096, factor=4, tau_f=0.5005, k_coarse=4, k0=8.0, u_rms=0.04, collision="mrt"):
+        self.nf, self.factor, self.tau_f, self.k_coarse = nf, factor, tau_f, k_coarse
+        self.nc = nf // factor
+        self.tau_c = 0.5 + (tau_f - 0.5) / factor
+        # f_neq scales with tau times the velocity gradient per cell: x factor on the coarse grid
+        self.neq_scale = factor * self.tau_c / tau_f
+        self.k0, self.u_rms, self.collision = k0, u_rms, collision
+
+    def fine(self, seed):
+        from .fluid import FluidSimulator
+        from .turbulence import random_velocity
+
+        s = FluidSimulator(self.nf, self.nf, mode="physics", scene="periodic", tau=self.tau_f,
+                           collision=self.collision)
+        ux, uy = random_velocity(self.nf, seed, self.k0, self.u_rms)
+        s.init_equilibrium(None, ux.astype(np.float32), uy.astype(np.float32))
+        return s
+
+    def coarse(self):
+        from .fluid import FluidSimulator
+
+        return FluidSimulator(self.nc, self.nc, mode="physics", scene="periodic", tau=self.tau_c,
+                              collision=self.collision)
+
+
+_W9 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+_EX = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1], dtype=np.float64)
+_EY = np.array([0, 0, -1, 0, 1, -1, -1, 1, 1], dtype=np.float64)
+
+
+def _neq_and_momentum(f):
+    """f: (9, ny, nx) absolute populations -> (f_neq, rho, jx, jy)."""
+    rho = f.sum(0)
+    jx = (f * _EX[:, None, None]).sum(0)
+    jy = (f * _EY[:, None, None]).sum(0)
+    ux, uy = jx / rho, jy / rho
+    eu = _EX[:, None, None] * ux + _EY[:, None, None] * uy
+    feq = _W9[:, None, None] * rho * (1 + 3 * eu + 4.5 * eu * eu - 1.5 * (ux * ux + uy * uy))
+    return f - feq, rho, jx, jy
+
+
+def _project(v):
+    s = v.sum(0)
+    sx = (v * _EX[:, None, None]).sum(0)
+    sy = (v * _EY[:, None, None]).sum(0)
+    return v - _W9[:, None, None] * (s + 3 * (_EX[:, None, None] * sx + _EY[:, None, None] * sy))
+
+
+def generate_pairs(closure, setup, seeds, snapshots=250, interval=80, crop=256, rng_seed=0, log=None):
+    """For every seed, run the fine lattice and add `snapshots` training pairs taken every
+    `interval` fine steps: features from the coarse-grained fine state advanced k_coarse
+    coarse steps, target the coarse-grained fine state k_coarse*factor fine steps later.
+    The feature and output scales are calibrated on the first pair (unit RMS)."""
+    rng = np.random.default_rng(rng_seed)
+    pred, target = setup.coarse(), setup.coarse()
+    kf = setup.k_coarse * setup.factor
+    assert interval >= kf
+    calibrated = False
+    for seed in seeds:
+        fine = setup.fine(seed)
+        for s in range(snapshots):
+            coarsen(fine, pred, setup.factor, setup.neq_scale)
+            pred.step(setup.k_coarse)
+            fine.step(kf)
+            coarsen(fine, target, setup.factor, setup.neq_scale)
+            if not calibrated:
+                fp = pred.read_populations(np.float64)
+                ft = target.read_populations(np.float64)
+                neq = _neq_and_momentum(fp)[0]
+                tgt = _project(ft - fp)
+                closure.set_scales(1.0 / max(float(neq.std()), 1e-12), 1.0 / max(float(tgt.std()), 1e-12))
+                calibrated = True
+            closure.add_pair(pred, target, int(rng.integers(0, setup.nc)), int(rng.integers(0, setup.nc)))
+            fine.step(interval - kf)
+        if log:
+            log("seed %d: %d pairs" % (seed, closure.npairs))
+        fine.close()
+    pred.close()
+    target.close()
+
+
+def coarse_velocity_of(sim_fine, factor):
+    """Momentum-weighted block average of the fine velocity field."""
+    f = sim_fine.read_populations(np.float64)
+    rho = f.sum(0)
+    jx = (f * _EX[:, None, None]).sum(0)
+    jy = (f * _EY[:, None, None]).sum(0)
+    ny, nx = rho.shape
+    blk = lambda a: a.reshape(ny // factor, factor, nx // factor, factor).mean(axis=(1, 3))
+    r = blk(rho)
+    return blk(jx) / r, blk(jy) / r
+
+
+def evaluate(closure, setup, seed, fine_steps=20000, check_every=2000):
+    """Run the fine lattice and two coarse lattices (without / with the closure) from the
+    coarse-grained initial state; relative L2 velocity error of each against the
+    coarse-grained fine run at every checkpoint."""
+    fine = setup.fine(seed)
+    plain, corr = setup.coarse(), setup.coarse()
+    coarsen(fine, plain, setup.factor, setup.neq_scale)
+    coarsen(fine, corr, setup.factor, setup.neq_scale)
+    rows = []
+    cs = check_every // setup.factor
+    assert cs % setup.k_coarse == 0
+    for t in range(check_every, fine_steps + 1, check_every):
+        fine.step(check_every)
+        plain.step(cs)
+        for _ in range(cs // setup.k_coarse):
+            corr.step(setup.k_coarse)
+            closure.apply(corr)
+        gx, gy = coarse_velocity_of(fine, setup.factor)
+        norm = np.sqrt(np.sum(gx * gx + gy * gy))
+        row = {"fine_step": t, "fine_nonfinite": fine.nonfinite_count()}
+        for name, s in (("plain", plain), ("closure", corr)):
+            _, ux, uy = s.read_macro()
+            row["err_" + name] = float(np.sqrt(np.sum((ux - gx) ** 2 + (uy - gy) ** 2)) / norm)
+        rows.append(row)
+    for s in (fine, plain, corr):
+        s.close()
+    return rows
+
+
+def time_runs(closure, setup, seed, fine_steps=20000):
+    """Device time (CUDA events on the lattices' streams, synchronised) of the plain fine
+    run, the plain coarse run and the coarse run with the closure, over the same span."""
+    import torch
+
+    out = {}
+    fine = setup.fine(seed)
+    plain, corr = setup.coarse(), setup.coarse()
+    coarsen(fine, plain, setup.factor, setup.neq_scale)
+    coarsen(fine, corr, setup.factor, setup.neq_scale)
+    stream = torch.cuda.Stream()
+    for s in (fine, plain, corr):
+        s.set_stream(stream.cuda_stream)
+    nc = fine_steps // setup.factor
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+
+    out["fine_s"] = timed(lambda: fine.step(fine_steps))
+    out["coarse_plain_s"] = timed(lambda: plain.step(nc))
+
+    def run_corr():
+        for _ in range(nc // setup.k_coarse):
+            corr.step(setup.k_coarse)
+            closure.apply(corr)
+
+    out["coarse_closure_s"] = timed(run_corr)
+    out["speedup_closure"] = out["fine_s"] / out["coarse_closure_s"]
+    out["speedup_plain"] = out["fine_s"] / out["coarse_plain_s"]
+    for s in (fine, plain, corr):
+        s.close()
+    return out

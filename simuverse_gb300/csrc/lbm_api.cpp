@@ -229,7 +229,7 @@ int validate_params(const lbm_params& p) {
     if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
     if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_VEC2) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
-    if (p.collision < LBM_COLLISION_BGK || p.collision > LBM_COLLISION_MRT)
+    if (p.collision < LBM_COLLISION_BGK || p.collision > LBM_COLLISION_KBC)
         return fail(LBM_ERR_ARG, "unknown collision %d", p.collision);
     if (p.collision != LBM_COLLISION_BGK && p.mode != LBM_MODE_PHYSICS)
         return fail(LBM_ERR_ARG, "reference mode is BGK only");

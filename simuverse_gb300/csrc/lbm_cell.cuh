@@ -19,10 +19,10 @@ constexpr double MRT_S_E = 1.1, MRT_S_EPS = 1.0, MRT_S_Q = 1.2;
 // Boundary rules on the pulled populations d (Zou-He inlet, anchored outflow), moments,
 // Guo forcing with countdown, BGK.  o receives the post-collision deviations; rho, ux, uy
 // the macroscopic values of the cell.
-template <class R>
+template <class R, int COLL = LBM_COLLISION_BGK>
 __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size_t c, uint16_t* __restrict__ flags,
                                              lbm_lattice_info* __restrict__ info, R omega, R (&o)[9], R& rho_out,
-                                             R& ux_out, R& uy_out, int collision = LBM_COLLISION_BGK) {
+                                             R& ux_out, R& uy_out) {
     const bool outlet = (m == LBM_OUTLET);
     if (m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
         const lbm_lattice_info in = info[c];
@@ -68,7 +68,50 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
     // w (drho + rho (4.5 (e.u)^2 - 1.5 u.u)) shared by the pair and an odd part 3 w rho e.u
     const R om = omega, om1 = R(1) - omega;
     const R r1 = rho * (R(3) * PW<R>(1)), r5 = rho * (R(3) * PW<R>(5));
-    if (collision == LBM_COLLISION_MRT) {
+    if (COLL == LBM_COLLISION_KBC) {
+        // entropic KBC (Karlin, Bosch & Chikatamarla 2014) on the natural moments: f = k + s + h
+        // with the shear part s from N = Pxx - Pyy and Pxy (s = N/4 on the x axis, -N/4 on the
+        // y axis, sigma lambda Pxy / 4 on the diagonals); f' = f - beta (2 ds + gamma dh),
+        // beta = omega / 2 (BGK's shear viscosity), gamma = 1/beta - (2 - 1/beta) <ds|dh> / <dh|dh>
+        // with <x|y> = sum x_i y_i / feq_i, i.e. the stabiliser that keeps the entropy
+        // production right; gamma = 2 is BGK.
+        R q[9];
+        {
+            const R e1 = ux, e2 = uy, e3 = ux + uy, e4 = ux - uy;
+            const R s1 = PW<R>(1) * (drho + rho * (R(4.5) * e1 * e1 - usq)), a1 = r1 * e1;
+            const R s2 = PW<R>(1) * (drho + rho * (R(4.5) * e2 * e2 - usq)), a2 = r1 * e2;
+            const R s3 = PW<R>(5) * (drho + rho * (R(4.5) * e3 * e3 - usq)), a3 = r5 * e3;
+            const R s4 = PW<R>(5) * (drho + rho * (R(4.5) * e4 * e4 - usq)), a4 = r5 * e4;
+            q[1] = s1 + a1; q[3] = s1 - a1;
+            q[4] = s2 + a2; q[2] = s2 - a2;
+            q[8] = s3 + a3; q[6] = s3 - a3;
+            q[5] = s4 + a4; q[7] = s4 - a4;
+            q[0] = PW<R>(0) * (drho - rho * usq);
+        }
+        R n[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) n[j] = d[j] - q[j];
+        const R dN = (n[1] + n[3]) - (n[2] + n[4]);
+        const R dP = (n[8] + n[6]) - (n[5] + n[7]);
+        R ds[9];
+        ds[0] = R(0);
+        ds[1] = ds[3] = R(0.25) * dN;
+        ds[2] = ds[4] = R(-0.25) * dN;
+        ds[8] = ds[6] = R(0.25) * dP;
+        ds[5] = ds[7] = R(-0.25) * dP;
+        R sh = R(0), hh = R(0);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const R dh = n[j] - ds[j];
+            const R inv_feq = recip_rn(PW<R>(j) + q[j]);
+            sh += ds[j] * dh * inv_feq;
+            hh += dh * dh * inv_feq;
+        }
+        const R beta = R(0.5) * om, ib = R(1) / beta;
+        const R gamma = hh > R(1e-30) ? ib - (R(2) - ib) * (sh / hh) : R(2);
+#pragma unroll
+        for (int j = 1; j < 9; ++j) o[j] = d[j] - beta * (R(2) * ds[j] + gamma * (n[j] - ds[j]));
+    } else if (COLL == LBM_COLLISION_MRT) {
         // multiple relaxation times on the orthogonal D2Q9 moments of Lallemand & Luo
         // (2000): energy e, energy square eps, energy fluxes qx, qy relax at fixed rates,
         // the stresses pxx, pxy at omega (same shear viscosity as BGK); density and
@@ -104,7 +147,7 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
         o[6] = d[6] + diag - cqx - cqy + cxy;
         o[5] = d[5] + diag + cqx - cqy - cxy;
         o[7] = d[7] + diag - cqx + cqy - cxy;
-    } else if (collision == LBM_COLLISION_REGULARIZED) {
+    } else if (COLL == LBM_COLLISION_REGULARIZED) {
         // regularised BGK: the non-equilibrium part is replaced by its projection on the
         // second-order Hermite moments before relaxation (same viscosity; the non-
         // hydrodynamic moments are reset every step)
@@ -185,11 +228,11 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
 
 // One cell (x, y) of a lattice of nx x ny cells whose rows are `pitch` elements apart
 // (pitch >= nx; the single-lattice kernel passes pitch = nx).
-template <class ST, bool MACRO>
+template <class ST, bool MACRO, int COLL = LBM_COLLISION_BGK>
 __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                  typename ST::R omega, int x, int y, int nx, int pitch, int ny,
-                                                 float* __restrict__ macro, int collision = LBM_COLLISION_BGK) {
+                                                 float* __restrict__ macro) {
     using R = typename ST::R;
     const size_t N = (size_t)pitch * ny;
     const unsigned c = (unsigned)y * (unsigned)pitch + (unsigned)x;  // cells < 2^31
@@ -232,7 +275,7 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
         }
     }
     R o[9], rho, ux, uy;
-    phys_collide<R>(d, m, fl, c, flags, info, omega, o, rho, ux, uy, collision);
+    phys_collide<R, COLL>(d, m, fl, c, flags, info, omega, o, rho, ux, uy);
     if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
 #pragma unroll
     for (int j = 0; j < 9; ++j) ST::st(B + (size_t)j * N + c, o[j]);

@@ -141,8 +141,7 @@ template <class ST, bool MACRO, int CPT = 4>
 __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                    typename ST::R omega, int x0, int y, int nx, int pitch, int ny,
-                                                   bool active, float* __restrict__ macro,
-                                                   int collision = LBM_COLLISION_BGK) {
+                                                   bool active, float* __restrict__ macro) {
     using R = typename ST::R;
     using T = typename ST::T;
     const int lane = threadIdx.x & 31;
@@ -239,7 +238,7 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             }
         }
         R o[9];
-        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k], collision);
+        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k]);
 #pragma unroll
         for (int j = 0; j < 9; ++j) d[j][k] = o[j];
     }

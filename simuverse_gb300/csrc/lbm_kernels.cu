@@ -226,15 +226,15 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
 // ------------------------------------------------------------------------------------
 // physics-mode step (cell update in lbm_cell.cuh)
 // ------------------------------------------------------------------------------------
-template <class ST, bool MACRO>
-__global__ void __launch_bounds__(TPB, 16) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
+// BGK and regularised fit 32 registers (full occupancy); MRT and KBC get 48
+template <class ST, bool MACRO, int COLL>
+__global__ void __launch_bounds__(TPB, (COLL == LBM_COLLISION_MRT || COLL == LBM_COLLISION_KBC) ? 10 : 16) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
-                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro,
-                                                   int collision) {
+                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro) {
     const int x = blockIdx.x * TPB + threadIdx.x;
     const int y = blockIdx.y;
     if (x >= nx) return;
-    phys_cell_update<ST, MACRO>(A, B, flags, info, omega, x, y, nx, nx, ny, macro, collision);
+    phys_cell_update<ST, MACRO, COLL>(A, B, flags, info, omega, x, y, nx, nx, ny, macro);
 }
 
 // ------------------------------------------------------------------------------------
@@ -444,14 +444,25 @@ cudaError_t launch_phys_init(lbm_handle* h, const float* r, const float* ux, con
     }
 }
 
-template <class ST, bool MACRO>
-static cudaError_t phys_step_t(lbm_handle* h, cudaStream_t s) {
+template <class ST, bool MACRO, int COLL>
+static cudaError_t phys_step_c(lbm_handle* h, cudaStream_t s) {
     using T = typename ST::T;
     using R = typename ST::R;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
-    k_phys_step<ST, MACRO><<<cell_grid(h), TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, omega, h->nx, h->ny, h->d_macro, h->p.collision);
+    k_phys_step<ST, MACRO, COLL><<<cell_grid(h), TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                              h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
+}
+
+// the collision is a compile-time choice so that each rule gets its own register budget
+template <class ST, bool MACRO>
+static cudaError_t phys_step_t(lbm_handle* h, cudaStream_t s) {
+    switch (h->p.collision) {
+        case LBM_COLLISION_REGULARIZED: return phys_step_c<ST, MACRO, LBM_COLLISION_REGULARIZED>(h, s);
+        case LBM_COLLISION_MRT: return phys_step_c<ST, MACRO, LBM_COLLISION_MRT>(h, s);
+        case LBM_COLLISION_KBC: return phys_step_c<ST, MACRO, LBM_COLLISION_KBC>(h, s);
+        default: return phys_step_c<ST, MACRO, LBM_COLLISION_BGK>(h, s);
+    }
 }
 
 cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
@@ -466,6 +477,14 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     }
     // auto = one cell per thread, the fastest variant measured on GB300 (86.8 % of the HBM
     // copy bandwidth at 4096^2 against 70.9 % for VEC4 and 68.6 % for BULK)
+    if (h->p.collision != LBM_COLLISION_BGK) {  // the vector kernels implement BGK only
+        switch (h->p.dtype) {
+            case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
+            case LBM_DTYPE_F64: return write_macro ? phys_step_t<StoreF64, true>(h, s) : phys_step_t<StoreF64, false>(h, s);
+            case LBM_DTYPE_F16: return write_macro ? phys_step_t<StoreF16, true>(h, s) : phys_step_t<StoreF16, false>(h, s);
+            default: return write_macro ? phys_step_t<StoreBF16, true>(h, s) : phys_step_t<StoreBF16, false>(h, s);
+        }
+    }
     if (h->p.kernel == LBM_KERNEL_BULK) return launch_phys_step_bulk(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);

@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(BULK_TPB) k_phys_step_bulk(const typename ST::
                                                              uint16_t* __restrict__ flags,
                                                              lbm_lattice_info* __restrict__ info, typename ST::R omega,
                                                              int nx, int ny, float* __restrict__ macro,
-                                                             int* __restrict__ status, int collision) {
+                                                             int* __restrict__ status) {
     using T = typename ST::T;
     using R = typename ST::R;
     using L = BulkLayout<ST>;
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(BULK_TPB) k_phys_step_bulk(const typename ST::
                     }
                 }
                 R o[9];
-                phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k], collision);
+                phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k]);
 #pragma unroll
                 for (int j = 0; j < 9; ++j) d[j][k] = o[j];
             }
@@ -373,7 +373,7 @@ static cudaError_t bulk_t(lbm_handle* h, cudaStream_t s) {
     k_phys_step_bulk<ST, MACRO><<<(unsigned)grid, BULK_TPB, L::SMEM, s>>>((const T*)h->buf[h->cur],
                                                                           (T*)h->buf[h->cur ^ 1], h->d_flags,
                                                                           h->d_info, omega, h->nx, h->ny, h->d_macro,
-                                                                          h->d_status, h->p.collision);
+                                                                          h->d_status);
     return cudaGetLastError();
 }
 

@@ -16,9 +16,9 @@ template <class ST, bool MACRO>
 __global__ void __launch_bounds__(VEC_TPB) k_phys_step_v4(const typename ST::T* __restrict__ A,
                                                           typename ST::T* __restrict__ B, uint16_t* __restrict__ flags,
                                                           lbm_lattice_info* __restrict__ info, typename ST::R omega,
-                                                          int nx, int ny, float* __restrict__ macro, int collision) {
+                                                          int nx, int ny, float* __restrict__ macro) {
     const int x0 = (blockIdx.x * VEC_TPB + threadIdx.x) * 4;
-    phys_cells4_update<ST, MACRO>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro, collision);
+    phys_cells4_update<ST, MACRO>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
 }
 
 // two cells per thread: one 32-bit access per plane for FP16 / BF16
@@ -28,9 +28,9 @@ __global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_v2(const typename ST:
                                                               uint16_t* __restrict__ flags,
                                                               lbm_lattice_info* __restrict__ info,
                                                               typename ST::R omega, int nx, int ny,
-                                                              float* __restrict__ macro, int collision) {
+                                                              float* __restrict__ macro) {
     const int x0 = (blockIdx.x * VEC_TPB + threadIdx.x) * 2;
-    phys_cells4_update<ST, MACRO, 2>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro, collision);
+    phys_cells4_update<ST, MACRO, 2>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
 }
 
 template <class ST, bool MACRO>
@@ -40,7 +40,7 @@ static cudaError_t phys_step_v2_t(lbm_handle* h, cudaStream_t s) {
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     const dim3 grid((unsigned)((h->nx / 2 + VEC_TPB - 1) / VEC_TPB), (unsigned)h->ny);
     k_phys_step_v2<ST, MACRO><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, omega, h->nx, h->ny, h->d_macro, h->p.collision);
+                                                        h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
 }
 
@@ -60,7 +60,7 @@ static cudaError_t phys_step_v4_t(lbm_handle* h, cudaStream_t s) {
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     const dim3 grid((unsigned)((h->nx / 4 + VEC_TPB - 1) / VEC_TPB), (unsigned)h->ny);
     k_phys_step_v4<ST, MACRO><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, omega, h->nx, h->ny, h->d_macro, h->p.collision);
+                                                        h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
 }
 
