@@ -378,6 +378,60 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_closure(args):
+    """Learned closure on periodic decaying turbulence: fine 4096^2 (tau 0.5005) against a
+    4x-coarsened 1024^2 lattice corrected by the trained BF16 network every k coarse steps.
+    Pairs from args.train_seeds seeds x args.snapshots snapshots x (fresh, rollout); with
+    --dagger N, N more rounds regenerate the pairs from closure-corrected rollouts and
+    continue training.  Evaluation on unseen seeds."""
+    import torch
+
+    import numpy as np
+
+    from simuverse_gb300.closure import Closure, TurbulenceSetup, evaluate, generate_pairs, time_runs
+
+    setup = TurbulenceSetup(nf=args.nx, factor=4, tau_f=0.5005, k_coarse=args.k_coarse, collision=args.collision)
+    out = {"workload": "closure", "fine": args.nx, "coarse": setup.nc, "tau_f": setup.tau_f, "tau_c": setup.tau_c,
+           "k_coarse": setup.k_coarse, "collision": args.collision}
+    c = Closure(setup.nc, setup.nc, seed=args.seed)
+    seeds = list(range(1000, 1000 + args.train_seeds))
+    npairs = args.train_seeds * args.snapshots * 2
+    curve = []
+    out["datagen_s"] = 0.0
+    out["train_s"] = 0.0
+    for rnd in range(1 + args.dagger):
+        c.reserve(npairs + 64, 256, 8)
+        t0 = time.perf_counter()
+        generate_pairs(c, setup, seeds, snapshots=args.snapshots, interval=args.interval, crop=256,
+                       rng_seed=args.seed + rnd, corrected=c if rnd > 0 else None, calibrate=rnd == 0)
+        out["datagen_s"] += time.perf_counter() - t0
+        hold = max(1, c.npairs // 20)
+        if rnd == 0:
+            out["pairs"] = c.npairs
+            out["scales"] = [c.s_in, c.s_out]
+            p0 = c.params
+            c.params = np.zeros_like(p0)
+            out["loss_zero_output"] = c.eval(c.npairs - hold, c.npairs)
+            c.params = p0
+            out["loss_initial"] = c.eval(c.npairs - hold, c.npairs)
+        t0 = time.perf_counter()
+        iters = args.train_iters if rnd == 0 else args.train_iters // 2
+        for block in range(args.train_blocks):
+            last = block >= args.train_blocks - 2
+            lt = c.train(iters // args.train_blocks, lr=args.lr / 4 if last else args.lr, seed=args.seed + 97 * rnd + block)
+            curve.append({"round": rnd, "iter": (block + 1) * (iters // args.train_blocks), "train_loss": lt,
+                          "heldout_loss": c.eval(c.npairs - hold, c.npairs)})
+        torch.cuda.synchronize()
+        out["train_s"] += time.perf_counter() - t0
+    out["training_curve"] = curve
+    out["eval"] = {}
+    for seed in args.eval_seeds:
+        rows = evaluate(c, setup, seed, fine_steps=args.steps, check_every=args.check_every)
+        out["eval"][str(seed)] = rows
+    out["timing"] = time_runs(c, setup, args.eval_seeds[0], fine_steps=args.steps)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,7 +443,18 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2"])
-    ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch", "closure"])
+    ap.add_argument("--train-seeds", type=int, default=8)
+    ap.add_argument("--snapshots", type=int, default=125)
+    ap.add_argument("--interval", type=int, default=160)
+    ap.add_argument("--dagger", type=int, default=1)
+    ap.add_argument("--k-coarse", type=int, default=4)
+    ap.add_argument("--train-iters", type=int, default=3000)
+    ap.add_argument("--train-blocks", type=int, default=10)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--eval-seeds", type=int, nargs="*", default=[9001, 9002])
+    ap.add_argument("--check-every", type=int, default=2000)
+    ap.add_argument("--collision", default="kbc", choices=["bgk", "kbc", "mrt", "regularized"])
     ap.add_argument("--taus", type=float, nargs="*", default=[0.51, 0.6, 0.9])
     ap.add_argument("--timing-steps", type=int, default=500)
     ap.add_argument("--domains", type=int, default=256)
@@ -404,6 +469,8 @@ def main():
         run_precision(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "closure":
+        run_closure(args)
     else:
         run_gpu(args)
 

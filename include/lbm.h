@@ -22,7 +22,7 @@
  *   lbm_set_info/get_info the info buffer            simuverse/src/fluid/lattice.rs:5-24
  *
  * The remaining entry points (populations, conservation sums, checkpoints, the batched
- * form) have no counterpart in the reference; each says so.
+ * form, the learned closure) have no counterpart in the reference; each says so.
  *
  * Conventions.  Every function returns an int status (LBM_OK = 0, negative on error,
  * LBM_IGNORED = 1 when the reference would silently ignore the request) and never
@@ -132,7 +132,7 @@ typedef struct lbm_params {
     int32_t macro_every_step;/* 1: write the macro field every step, as the reference does;
                                 0: only on the last step of each lbm_step call */
     int32_t kernel;          /* LBM_KERNEL_*: step kernel variant (results agree to rounding) */
-    int32_t collision;       /* physics mode: LBM_COLLISION_BGK or LBM_COLLISION_REGULARIZED */
+    int32_t collision;       /* physics mode: LBM_COLLISION_* */
     int32_t reserved[4];
 } lbm_params;
 
@@ -168,6 +168,24 @@ int lbm_add_obstacle(lbm_handle* h, int32_t x, int32_t y);
 int lbm_touch_begin(lbm_handle* h);
 int lbm_touch_move(lbm_handle* h, float px, float py);
 int lbm_add_external_force(lbm_handle* h, float pos_x, float pos_y, float pre_x, float pre_y);
+
+/* batched interaction on the GPU -- no single counterpart in the reference, which writes
+   mask rows and records from the host one event at a time (d2q9_node.rs:215-300).  The
+   list is applied in order with the result of the same sequence of single calls above
+   (including the touch state), but the mask is written by two kernels on the handle's
+   stream from a compact edit list and the call does not wait for the GPU.  applied (may be
+   NULL) receives the number of edits that wrote the mask.  On an error nothing is applied. */
+#define LBM_EDIT_OBSTACLE 0    /* a, b: lattice cell (lbm_add_obstacle) */
+#define LBM_EDIT_CLICK 1       /* a, b: canvas pixel (lbm_on_click) */
+#define LBM_EDIT_FORCE 2       /* a, b: position, c, d: previous position, canvas pixels
+                                  (lbm_add_external_force) */
+#define LBM_EDIT_TOUCH_BEGIN 3 /* lbm_touch_begin */
+#define LBM_EDIT_TOUCH_MOVE 4  /* a, b: canvas pixel (lbm_touch_move) */
+typedef struct lbm_edit {
+    int32_t kind;
+    float a, b, c, d;
+} lbm_edit;
+int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* applied);
 
 /* host-only mask helpers (no GPU needed; the handle functions above use the same code).
    lbm_build_mask: the scene mask of p (init_lattice_material, lattice.rs:26-98, for the
@@ -246,6 +264,63 @@ int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches);
 int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy);
 
 /* ---------------------------------------------------------------------------------
+   Consumers of the macro field, on the device (no texture or graphics interop).  Each
+   reads the field the last lbm_step wrote, rounded to FP16 as the reference's
+   rgba16float macro_tex holds it; before the first step the field is zero.
+   --------------------------------------------------------------------------------- */
+
+/* tracer particles -- the particle buffer and canvas of SettingObj (setting/setting_obj.rs)
+   and the particle_update.wgsl dispatch FluidSimulator::compute runs after each step
+   (fluid/fluid_simulator.rs:217-232) */
+typedef struct lbm_particle_params {
+    int32_t canvas_w, canvas_h; /* canvas pixels; canvas / pixel_size must give the lattice */
+    int32_t count;              /* requested particles; the grid is lbm_particles_grid's */
+    float life_time;            /* steps a particle lives before it restarts at its initial position */
+    int32_t point_size;         /* side of the splatted square, pixels */
+    float speed_factor;         /* pixels moved per lattice velocity unit (4.15 in the reference) */
+    float fade_out_factor;      /* canvas alpha fade per present (0.96) */
+    int32_t color_ty;           /* present colour: 0 direction hue, 1 speed hue, 2 uniform colour */
+    float color[4];             /* uniform colour (color_ty 2) */
+    uint64_t seed;              /* initial jitter (the reference draws from an unseeded generator) */
+    int32_t deterministic;      /* 1: overlapping splats go to the highest particle index;
+                                   0: plain racing stores, as the reference's dispatch */
+    int32_t reserved[3];
+} lbm_particle_params;
+
+typedef struct lbm_particles lbm_particles;
+
+void lbm_particle_params_default(lbm_particle_params* p);
+/* get_particles_data (lib.rs:248-276): num_x = ceil(sqrt(count * w / h)), num_y = ceil(num_x * h / w) */
+int lbm_particles_grid(int32_t canvas_w, int32_t canvas_h, int32_t count, int32_t* num_x, int32_t* num_y);
+/* init_trajectory_particles (lib.rs:278-316) on the host: num_x * num_y records of 6 floats
+   (pos x, pos y, initial x, initial y, life, fade), the reference's TrajectoryParticle;
+   grid column x, row y is record x * num_y + y */
+int lbm_particles_init_state(const lbm_particle_params* p, int32_t num_x, int32_t num_y, float* out);
+int lbm_particles_create(lbm_handle* h, const lbm_particle_params* p, lbm_particles** out);
+int lbm_particles_destroy(lbm_particles* ps);
+int lbm_particles_info(const lbm_particles* ps, int32_t* num_x, int32_t* num_y);
+/* one particle_update.wgsl pass over every particle, on h's stream */
+int lbm_particles_update(lbm_particles* ps, lbm_handle* h);
+/* present.wgsl (assets/wgsl/present.wgsl:15-54): RGBA (4 floats per pixel) of the canvas,
+   then the alpha fade; *d_rgba (may be NULL) receives the device buffer */
+int lbm_particles_present(lbm_particles* ps, lbm_handle* h, float** d_rgba);
+int lbm_particles_read(lbm_particles* ps, float* out);
+int lbm_particles_write(lbm_particles* ps, const float* in);
+/* canvas: 3 floats per pixel (alpha, vx, vy), the reference's Pixel; rgba: the last present */
+int lbm_particles_read_canvas(lbm_particles* ps, float* canvas, float* rgba);
+int lbm_particles_counters(const lbm_particles* ps, uint64_t* updates, uint64_t* launches);
+
+/* curl_update.wgsl:12-33: N floats, curl * 3.5 + 0.5 rounded to FP16, into a device buffer */
+int lbm_curl(lbm_handle* h, float* d_out);
+
+/* field colour maps, one RGBA (4 floats) per canvas pixel into a device buffer, the field
+   sampled with linear filtering and clamp-to-edge addressing at each pixel centre */
+#define LBM_COLOR_CURL 0  /* lbm/present.wgsl:18-40: hue curl, saturation 0.6 + 1.4 speed,
+                             value 0.6 + 0.33 rho, alpha rho (d_curl from lbm_curl) */
+#define LBM_COLOR_ANGLE 1 /* lbm/blend_img.wgsl:11-16: hue of atan2(ux, uy), opaque */
+int lbm_colorize(lbm_handle* h, int32_t mode, const float* d_curl, int32_t canvas_w, int32_t canvas_h, float* d_rgba);
+
+/* ---------------------------------------------------------------------------------
    Batched form -- no counterpart in the reference (simuverse runs one lattice).  Many
    independent physics-mode FP32 lattices (moving-lid cavities and channels) of uneven
    size advance together: in one cooperative persistent launch per lbm_batch_step call,
@@ -303,6 +378,51 @@ int lbm_batch_read_populations(lbm_batch* b, int32_t i, float* f);
 int lbm_batch_read_info(lbm_batch* b, int32_t i, lbm_lattice_info* info);
 int lbm_batch_conservation(lbm_batch* b, int32_t i, double out[3]);
 int lbm_batch_counters(const lbm_batch* b, uint64_t* steps, uint64_t* launches);
+
+/* ---------------------------------------------------------------------------------
+   Learned closure of a coarsened lattice -- no counterpart in the reference.  A
+   three-layer 3x3 convolution (9 -> 32 -> 32 -> 9 channels; BF16 weights and activations,
+   FP32 accumulation on the tensor cores) maps s_in * f_neq of every coarse cell to a
+   correction delta = P(y) / s_out of its populations; P removes the density and momentum
+   of the correction, so no cell's rho or j changes.  Trained on the GPU (own forward,
+   backward and Adam kernels) on pairs (coarse state C after k coarse steps from a
+   coarse-grained fine state, coarse-grained fine state C* k * factor fine steps later),
+   target s_out * P(C* - C), loss over the interior of square crops.  Closure lattices
+   are physics-mode FP32 handles of the closure's size.
+   --------------------------------------------------------------------------------- */
+typedef struct lbm_closure lbm_closure;
+
+/* number of logical parameters: W1[9][9][32], b1[32], W2[9][32][32], b2[32], W3[9][32][9],
+   b3[9] ([tap][cin][cout]; tap 3 * (dy + 1) + (dx + 1) reads input cell (x + dx, y + dy)) */
+int lbm_closure_param_count(void);
+/* nx a multiple of 16; He-initialised from seed */
+int lbm_closure_create(int32_t nx, int32_t ny, uint64_t seed, lbm_closure** out);
+int lbm_closure_destroy(lbm_closure* c);
+int lbm_closure_set_scales(lbm_closure* c, float s_in, float s_out);
+int lbm_closure_get_params(lbm_closure* c, float* out);
+int lbm_closure_set_params(lbm_closure* c, const float* in);
+/* coarse = block average over factor x factor cells of the fine lattice's density and
+   momentum, equilibrium of those, plus neq_scale times the block-averaged f_neq */
+int lbm_coarsen(lbm_handle* fine, lbm_handle* coarse, int32_t factor, float neq_scale);
+/* adds the network's correction to h's current populations (periodic convolution),
+   asynchronously on h's stream */
+int lbm_closure_apply(lbm_closure* c, lbm_handle* h);
+/* correction of the whole lattice without applying it: 9 planes of nx * ny floats */
+int lbm_closure_predict(lbm_closure* c, lbm_handle* h, float* delta_out);
+/* training storage: up to max_pairs pairs of crop x crop windows, batches of `batch` */
+int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t batch);
+/* stores the crop at (ox, oy) (periodic) of the pair (pred, target) */
+int lbm_closure_add_pair(lbm_closure* c, lbm_handle* pred, lbm_handle* target, int32_t ox, int32_t oy);
+int lbm_closure_pairs(const lbm_closure* c, int32_t* n);
+/* Adam on random batches; loss_out (may be NULL): mean loss of the last iteration */
+int lbm_closure_train(lbm_closure* c, int32_t iters, float lr, uint64_t seed, double* loss_out);
+/* mean loss over stored pairs [begin, end), parameters unchanged */
+int lbm_closure_eval(lbm_closure* c, int32_t begin, int32_t end, double* loss_out);
+/* forward + backward on host crops feats, targets ([nimg][size][size][9], feature and
+   output units); grads: lbm_closure_param_count() floats */
+int lbm_closure_loss_grad(lbm_closure* c, int32_t nimg, int32_t size, const float* feats, const float* targets,
+                          double* loss_out, float* grads);
+int lbm_closure_counters(const lbm_closure* c, uint64_t* launches, uint64_t* adam_steps);
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,13 @@ def lib() -> ctypes.CDLL:
             "lo_mask_physics_channel": ([_I, _I, _F, ctypes.c_uint64, _F, _F, _F, _P], _I),
             "lo_conservation_dev_f32": ([_I, _I, _P, _P, _P], None),
             "lo_conservation_dev_f64": ([_I, _I, _P, _P, _P], None),
+            "lo_h16": ([_F], _F),
+            "lo_particles_grid": ([_I, _I, _I, _P, _P], None),
+            "lo_particles_init": ([_I, _I, _I, _I, _F, ctypes.c_uint64, _P], None),
+            "lo_particles_update": ([_I, _I, _P, _P, _I, _F, _F, _F, _I, _I, _I, _I, _I, _P, _P], None),
+            "lo_present_canvas": ([_I, _I, _I, _F, _P, _P, _P], None),
+            "lo_curl": ([_I, _I, _P, _P, _I, _P], None),
+            "lo_colorize": ([_I, _I, _P, _P, _P, _P, _I, _I, _I, _P], None),
             "lo_num_threads": ([], _I),
             "lo_set_num_threads": ([_I], None),
         }
@@ -229,3 +236,61 @@ def num_threads():
 
 def set_num_threads(n):
     lib().lo_set_num_threads(int(n))
+
+
+# ---------------------------------------------------------------------------------------
+# consumers of the macro field (lbm_oracle_view.inc)
+# ---------------------------------------------------------------------------------------
+def particles_grid(cw, ch, count):
+    a, b = ctypes.c_int(), ctypes.c_int()
+    lib().lo_particles_grid(cw, ch, count, ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def particles_init(cw, ch, num_x, num_y, life_time, seed):
+    out = np.empty((num_x * num_y, 6), np.float32)
+    lib().lo_particles_init(cw, ch, num_x, num_y, float(life_time), int(seed), _p(out))
+    return out
+
+
+def particles_update(ux, uy, zero, lattice_pixel, life_time, speed_factor, point_size, cw, ch, poiseuille, state,
+                     canvas):
+    """One particle_update.wgsl pass; state (n, 6) and canvas (ch, cw, 3) float32, in place."""
+    ny, nx = ux.shape
+    ux = np.ascontiguousarray(ux, np.float32)
+    uy = np.ascontiguousarray(uy, np.float32)
+    assert state.dtype == np.float32 and state.flags.c_contiguous and canvas.dtype == np.float32
+    lib().lo_particles_update(nx, ny, _p(ux), _p(uy), int(zero), float(lattice_pixel), float(life_time),
+                              float(speed_factor), int(point_size), cw, ch, int(poiseuille), state.shape[0],
+                              _p(state), _p(canvas))
+
+
+def present_canvas(canvas, color_ty, speed_ty, fade_out, rgb=(1.0, 1.0, 1.0)):
+    """present.wgsl over the canvas (ch, cw, 3) in place; returns RGBA (ch, cw, 4)."""
+    ch, cw, _ = canvas.shape
+    rgba = np.empty((ch, cw, 4), np.float32)
+    col = np.asarray(rgb, np.float32)
+    lib().lo_present_canvas(cw * ch, int(color_ty), int(speed_ty), float(fade_out), _p(col), _p(canvas), _p(rgba))
+    return rgba
+
+
+def curl(ux, uy, zero=False):
+    ny, nx = ux.shape
+    ux = np.ascontiguousarray(ux, np.float32)
+    uy = np.ascontiguousarray(uy, np.float32)
+    out = np.empty((ny, nx), np.float32)
+    lib().lo_curl(nx, ny, _p(ux), _p(uy), int(zero), _p(out))
+    return out
+
+
+def colorize(rho, ux, uy, curl_field, cw, ch, mode, zero=False):
+    """mode 0: curl hue, 1: velocity-angle hue; fields are the FP32 macro planes."""
+    ny, nx = ux.shape
+    planes = []
+    for a in (rho, ux, uy):
+        a = np.zeros((ny, nx), np.float32) if zero else np.asarray(a, np.float32).astype(np.float16).astype(np.float32)
+        planes.append(np.ascontiguousarray(a))
+    c = None if curl_field is None else np.ascontiguousarray(curl_field, np.float32)
+    rgba = np.empty((ch, cw, 4), np.float32)
+    lib().lo_colorize(nx, ny, _p(planes[0]), _p(planes[1]), _p(planes[2]), _p(c), cw, ch, int(mode), _p(rgba))
+    return rgba

@@ -1,6 +1,6 @@
 """Build recipe for the oracle (test infrastructure, not product code).
 
-Compiles oracle/lbm_oracle.c into oracle/_build/liblbm_oracle.so with OpenMP and with
+Compiles oracle/lbm_oracle.c (with the .inc files it includes) into oracle/_build/liblbm_oracle.so with OpenMP and with
 floating-point contraction disabled, so that every float operation of the restatement
 rounds exactly where the WGSL expression it follows rounds.  No architecture-specific
 flags: the same source builds on the x86_64 build host and on the aarch64 GPU host.
@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liblbm_oracle.so")
 SOURCES = ["lbm_oracle.c"]
-DEPS = SOURCES + ["lbm_oracle.h", "lbm_oracle_phys.inc"]
+DEPS = SOURCES + ["lbm_oracle.h", "lbm_oracle_phys.inc", "lbm_oracle_view.inc"]
 
 
 def _stale() -> bool:

@@ -420,3 +420,8 @@ int lo_mask_physics_channel(int nx, int ny, float u_max, uint64_t seed, float so
 #include "lbm_oracle_phys.inc"
 #undef LO_REAL
 #undef LO_SFX
+
+/* ------------------------------------------------------------------------- */
+/* consumers of the macro field: particles, canvas, curl, colour maps        */
+/* ------------------------------------------------------------------------- */
+#include "lbm_oracle_view.inc"

@@ -89,6 +89,21 @@ int lo_mask_physics_channel(int nx, int ny, float u_max, uint64_t seed, float so
 void lo_conservation_dev_f32(int nx, int ny, const lo_info* info, const float* A, double out[3]);
 void lo_conservation_dev_f64(int nx, int ny, const lo_info* info, const double* A, double out[3]);
 
+/* ---------------- consumers of the macro field (lbm_oracle_view.inc) ---------------- */
+float lo_h16(float v); /* nearest FP16 value, ties to even */
+void lo_particles_grid(int cw, int ch, int count, int* num_x, int* num_y);
+/* records of 6 floats: pos x, pos y, initial x, initial y, life, fade */
+void lo_particles_init(int cw, int ch, int num_x, int num_y, float life_time, uint64_t seed, float* out);
+/* ux, uy: the FP32 macro planes (rounded to FP16 inside); zero: no step since init */
+void lo_particles_update(int nx, int ny, const float* ux, const float* uy, int zero, float lattice_pixel,
+                         float life_time, float speed_factor, int point_size, int cw, int ch, int poiseuille,
+                         int count, float* state, float* canvas);
+void lo_present_canvas(int npix, int color_ty, int speed_ty, float fade_out, const float* rgb, float* canvas,
+                       float* rgba);
+void lo_curl(int nx, int ny, const float* ux, const float* uy, int zero, float* out);
+void lo_colorize(int nx, int ny, const float* rho16, const float* ux16, const float* uy16, const float* curl, int cw,
+                 int ch, int mode, float* rgba);
+
 /* number of OpenMP threads the oracle uses */
 int lo_num_threads(void);
 void lo_set_num_threads(int n);

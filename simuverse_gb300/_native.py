@@ -46,6 +46,24 @@ class LbmParams(ctypes.Structure):
     ]
 
 
+class ParticleParams(ctypes.Structure):
+    _fields_ = [("canvas_w", ctypes.c_int32), ("canvas_h", ctypes.c_int32), ("count", ctypes.c_int32),
+                ("life_time", ctypes.c_float), ("point_size", ctypes.c_int32), ("speed_factor", ctypes.c_float),
+                ("fade_out_factor", ctypes.c_float), ("color_ty", ctypes.c_int32), ("color", ctypes.c_float * 4),
+                ("seed", ctypes.c_uint64), ("deterministic", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+
+COLOR_MODES = {"curl": 0, "angle": 1}
+
+
+class Edit(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("a", ctypes.c_float), ("b", ctypes.c_float), ("c", ctypes.c_float),
+                ("d", ctypes.c_float)]
+
+
+EDITS = {"obstacle": 0, "click": 1, "force": 2, "touch_begin": 3, "touch_move": 4}
+
+
 class DomainDesc(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("scene", ctypes.c_int32),
                 ("tau", ctypes.c_float), ("speed", ctypes.c_float), ("reserved", ctypes.c_int32 * 3)]
@@ -105,6 +123,20 @@ _SIGNATURES = {
     "lbm_save": [_P, ctypes.c_char_p],
     "lbm_load": [_P, ctypes.c_char_p],
     "lbm_conservation_noalloc": [_P, _I, _I, _P, _I, _I, _P, _P],
+    "lbm_apply_edits": [_P, _P, _I, ctypes.POINTER(_I)],
+    "lbm_particles_grid": [_I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)],
+    "lbm_particles_init_state": [_P, _I, _I, _P],
+    "lbm_particles_create": [_P, _P, ctypes.POINTER(_P)],
+    "lbm_particles_destroy": [_P],
+    "lbm_particles_info": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)],
+    "lbm_particles_update": [_P, _P],
+    "lbm_particles_present": [_P, _P, ctypes.POINTER(_P)],
+    "lbm_particles_read": [_P, _P],
+    "lbm_particles_write": [_P, _P],
+    "lbm_particles_read_canvas": [_P, _P, _P],
+    "lbm_particles_counters": [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
+    "lbm_curl": [_P, _P],
+    "lbm_colorize": [_P, _I, _P, _I, _I, _P],
     "lbm_closure_create": [_I, _I, ctypes.c_uint64, ctypes.POINTER(_P)],
     "lbm_closure_destroy": [_P],
     "lbm_closure_set_scales": [_P, _F, _F],
@@ -161,6 +193,8 @@ def load() -> ctypes.CDLL:
     lib.lbm_closure_param_count.argtypes = []
     lib.lbm_params_default.restype = None
     lib.lbm_params_default.argtypes = [ctypes.POINTER(LbmParams)]
+    lib.lbm_particle_params_default.restype = None
+    lib.lbm_particle_params_default.argtypes = [ctypes.POINTER(ParticleParams)]
     for name, args in _SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = ctypes.c_int
@@ -183,4 +217,5 @@ def ptr(a: np.ndarray) -> ctypes.c_void_p:
 
 def exported_symbols():
     """Names declared in include/lbm.h that the library must export."""
-    return ["lbm_abi_version", "lbm_last_error", "lbm_params_default", "lbm_closure_param_count"] + list(_SIGNATURES)
+    return ["lbm_abi_version", "lbm_last_error", "lbm_params_default", "lbm_closure_param_count",
+            "lbm_particle_params_default"] + list(_SIGNATURES)

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "liblbm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["lbm_kernels.cu", "lbm_step_vec.cu", "lbm_step_bulk.cu", "lbm_batch.cu", "lbm_noalloc.cu", "lbm_closure.cu", "lbm_api.cpp"]
+SOURCES = ["lbm_kernels.cu", "lbm_step_vec.cu", "lbm_step_bulk.cu", "lbm_batch.cu", "lbm_noalloc.cu", "lbm_closure.cu", "lbm_view.cu", "lbm_api.cpp"]
 
 
 def _nvcc() -> str:

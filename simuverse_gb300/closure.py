@@ -158,21 +158,35 @@ def _project(v):
     return v - _W9[:, None, None] * (s + 3 * (_EX[:, None, None] * sx + _EY[:, None, None] * sy))
 
 
-def generate_pairs(closure, setup, seeds, snapshots=250, interval=80, crop=256, rng_seed=0, log=None):
-    """For every seed, run the fine lattice and add `snapshots` training pairs taken every
-    `interval` fine steps: features from the coarse-grained fine state advanced k_coarse
-    coarse steps, target the coarse-grained fine state k_coarse*factor fine steps later.
-    The feature and output scales are calibrated on the first pair (unit RMS)."""
+def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256, rng_seed=0, log=None,
+                   sources=("fresh", "rollout"), corrected=None, calibrate=True):
+    """Training pairs from `snapshots` snapshots of every seed, taken every `interval` fine
+    steps over one fine run.  Each snapshot adds one pair per source:
+
+    * "fresh": the coarse-grained fine state advanced k_coarse coarse steps;
+    * "rollout": a coarse lattice that has run alongside the fine one since the coarse-grained
+      initial state -- with the closure `corrected` applied every k_coarse coarse steps when
+      given, as in evaluation -- so the pairs cover the states a long coarse run reaches.
+
+    The target is the coarse-grained fine state at the same time.  With `calibrate`, the
+    feature and output scales are set from the first fresh pair (unit RMS)."""
     rng = np.random.default_rng(rng_seed)
     pred, target = setup.coarse(), setup.coarse()
     kf = setup.k_coarse * setup.factor
-    assert interval >= kf
-    calibrated = False
+    assert interval % kf == 0 and interval >= kf
+    calibrated = not calibrate
     for seed in seeds:
         fine = setup.fine(seed)
+        roll = None
+        if "rollout" in sources:
+            roll = setup.coarse()
+            coarsen(fine, roll, setup.factor, setup.neq_scale)
         for s in range(snapshots):
-            coarsen(fine, pred, setup.factor, setup.neq_scale)
-            pred.step(setup.k_coarse)
+            if "fresh" in sources:
+                coarsen(fine, pred, setup.factor, setup.neq_scale)
+                pred.step(setup.k_coarse)
+            if roll is not None:
+                roll.step(setup.k_coarse)
             fine.step(kf)
             coarsen(fine, target, setup.factor, setup.neq_scale)
             if not calibrated:
@@ -182,11 +196,23 @@ def generate_pairs(closure, setup, seeds, snapshots=250, interval=80, crop=256, 
                 tgt = _project(ft - fp)
                 closure.set_scales(1.0 / max(float(neq.std()), 1e-12), 1.0 / max(float(tgt.std()), 1e-12))
                 calibrated = True
-            closure.add_pair(pred, target, int(rng.integers(0, setup.nc)), int(rng.integers(0, setup.nc)))
+            ox, oy = int(rng.integers(0, setup.nc)), int(rng.integers(0, setup.nc))
+            if "fresh" in sources:
+                closure.add_pair(pred, target, ox, oy)
+            if roll is not None:
+                closure.add_pair(roll, target, ox, oy)
+                if corrected is not None:
+                    corrected.apply(roll)
+                for _ in range((interval - kf) // kf):
+                    roll.step(setup.k_coarse)
+                    if corrected is not None:
+                        corrected.apply(roll)
             fine.step(interval - kf)
         if log:
             log("seed %d: %d pairs" % (seed, closure.npairs))
         fine.close()
+        if roll is not None:
+            roll.close()
     pred.close()
     target.close()
 

@@ -9,6 +9,7 @@
 //                                simuverse/src/fluid/fluid_simulator.rs:137-193
 // Built with -ffp-contract=off so that the float geometry of the masks and force strokes
 // rounds as the Rust code does.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -254,6 +255,9 @@ int upload_info_rows(lbm_handle* h, int y0, int y1) {
     const size_t off = (size_t)y0 * h->nx, cnt = (size_t)(y1 - y0) * h->nx;
     LBM_CK(cudaMemcpyAsync(h->d_info + off, h->host_info.data() + off, cnt * sizeof(lbm_lattice_info),
                            cudaMemcpyHostToDevice, h->stream));
+    if (h->host_mirror_valid)  // the uploaded rows are rows of the host copy
+        LBM_CK(cudaMemcpyAsync(h->d_host_info + off, h->d_info + off, cnt * sizeof(lbm_lattice_info),
+                               cudaMemcpyDeviceToDevice, h->stream));
     return LBM_OK;
 }
 
@@ -289,6 +293,8 @@ void free_all(lbm_handle* h) {
     cudaFree(h->d_part);
     cudaFree(h->d_count);
     cudaFree(h->d_status);
+    cudaFree(h->d_host_info);
+    cudaFree(h->d_edits);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
@@ -520,6 +526,123 @@ int lbm_add_external_force(lbm_handle* h, float pos_x, float pos_y, float pre_x,
     }
     LBM_TRY(rebuild_flags(h));
     return sync(h);
+}
+
+int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* applied) {
+    LBM_TRY(check_handle(h));
+    if (n < 0 || (n > 0 && !edits)) return fail(LBM_ERR_ARG, "bad edit list");
+    // resolve the list on the host exactly as the single calls would (guards, touch state,
+    // stroke geometry), then let two kernels write the device mask
+    float pre_x = h->pre_x, pre_y = h->pre_y;
+    std::vector<lbm::EditObstacle> obs;
+    std::vector<lbm::EditForce> forces;
+    int32_t count = 0;
+    const int r = (int)OBSTACLE_RADIUS;
+    auto stroke = [&](float px, float py, float qx, float qy, int seq) {
+        std::vector<size_t> cells;
+        const lbm_lattice_info rec = force_stroke(h->nx, h->ny, h->p.pixel_size, px, py, qx, qy, cells);
+        for (size_t c : cells) forces.push_back({(uint32_t)c, seq, rec.vx, rec.vy});
+        ++count;
+    };
+    for (int32_t i = 0; i < n; ++i) {
+        const lbm_edit& e = edits[i];
+        switch (e.kind) {
+            case LBM_EDIT_OBSTACLE: {
+                const int x = (int)e.a, y = (int)e.b;
+                if ((float)x != e.a || (float)y != e.b || x < 0 || x >= h->nx || y - r < 0 || y + r > h->ny)
+                    return fail(LBM_ERR_ARG, "edit %d: obstacle at (%g, %g) outside the lattice", i, e.a, e.b);
+                obs.push_back({x, y, i, 0});
+                ++count;
+                break;
+            }
+            case LBM_EDIT_CLICK: {  // lbm_on_click
+                if (e.a <= 0.0f || e.b <= 0.0f) break;
+                const unsigned ps = (unsigned)h->p.pixel_size;
+                const unsigned x = (unsigned)e.a / ps, y = (unsigned)e.b / ps;
+                const unsigned half = (unsigned)OBSTACLE_RADIUS;
+                if (x < half || (long)x >= (long)h->nx - (long)(half + 2) || y < half ||
+                    (long)y >= (long)h->ny - (long)(half + 2))
+                    break;
+                obs.push_back({(int)x, (int)y, i, 0});
+                ++count;
+                break;
+            }
+            case LBM_EDIT_FORCE:
+                if (h->p.pixel_size < 2) return fail(LBM_ERR_ARG, "edit %d: force strokes need pixel_size >= 2", i);
+                stroke(e.a, e.b, e.c, e.d, i);
+                break;
+            case LBM_EDIT_TOUCH_BEGIN: pre_x = pre_y = 0.0f; break;
+            case LBM_EDIT_TOUCH_MOVE: {  // lbm_touch_move
+                if (e.a <= 0.0f || e.b <= 0.0f) {
+                    pre_x = pre_y = 0.0f;
+                    break;
+                }
+                const float dx = e.a - pre_x, dy = e.b - pre_y;
+                const float dis = std::sqrt(dx * dx + dy * dy);
+                if (!((pre_x == 0.0f && pre_y == 0.0f) || dis > 300.0f)) {
+                    if (h->p.pixel_size < 2)
+                        return fail(LBM_ERR_ARG, "edit %d: force strokes need pixel_size >= 2", i);
+                    stroke(e.a, e.b, pre_x, pre_y, i);
+                }
+                pre_x = e.a;
+                pre_y = e.b;
+                break;
+            }
+            default: return fail(LBM_ERR_ARG, "edit %d: unknown kind %d", i, e.kind);
+        }
+    }
+    LBM_TRY(use_device(h));
+    // a cell written by several strokes keeps the last one
+    if (forces.size() > 1) {
+        std::vector<size_t> order(forces.size());
+        for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](size_t a, size_t b) { return forces[a].cell < forces[b].cell; });
+        std::vector<lbm::EditForce> last;
+        for (size_t k = 0; k < order.size(); ++k)
+            if (k + 1 == order.size() || forces[order[k + 1]].cell != forces[order[k]].cell)
+                last.push_back(forces[order[k]]);
+        forces.swap(last);
+    }
+    if (!h->host_mirror_valid && !obs.empty()) {
+        if (!h->d_host_info) LBM_CK(cudaMalloc((void**)&h->d_host_info, h->N * sizeof(lbm_lattice_info)));
+        LBM_CK(cudaMemcpyAsync(h->d_host_info, h->host_info.data(), h->N * sizeof(lbm_lattice_info),
+                               cudaMemcpyHostToDevice, h->stream));
+        h->host_mirror_valid = true;
+    }
+    const size_t bytes = obs.size() * sizeof(lbm::EditObstacle) + forces.size() * sizeof(lbm::EditForce);
+    if (bytes > 0) {
+        if (bytes > h->edits_cap) {
+            LBM_CK(cudaStreamSynchronize(h->stream));  // the old list may still be read
+            cudaFree(h->d_edits);
+            h->d_edits = nullptr;
+            h->edits_cap = 0;
+            const size_t cap = std::max(bytes, (size_t)4096);
+            LBM_CK(cudaMalloc(&h->d_edits, cap));
+            h->edits_cap = cap;
+        }
+        std::vector<unsigned char> stage(bytes);
+        std::memcpy(stage.data(), obs.data(), obs.size() * sizeof(lbm::EditObstacle));
+        std::memcpy(stage.data() + obs.size() * sizeof(lbm::EditObstacle), forces.data(),
+                    forces.size() * sizeof(lbm::EditForce));
+        LBM_CK(cudaMemcpyAsync(h->d_edits, stage.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+        int row0 = h->ny, row1 = 0;
+        for (const auto& o : obs) {
+            row0 = std::min(row0, o.y - r);
+            row1 = std::max(row1, o.y + r);
+            obstacle_disc(h->nx, o.x, o.y, h->host_info.data());  // D2Q9Node::lattice_info_data
+        }
+        const auto* d_obs = (const lbm::EditObstacle*)h->d_edits;
+        const auto* d_forces = (const lbm::EditForce*)((const unsigned char*)h->d_edits +
+                                                        obs.size() * sizeof(lbm::EditObstacle));
+        LBM_CK(lbm::launch_edits(h, d_obs, (int)obs.size(), d_forces, (int)forces.size(), row0, row1, h->stream));
+        h->launches += (obs.empty() ? 0 : 1) + (forces.empty() ? 0 : 1);
+        LBM_TRY(rebuild_flags(h));
+    }
+    h->pre_x = pre_x;
+    h->pre_y = pre_y;
+    if (applied) *applied = count;
+    return LBM_OK;
 }
 
 int lbm_build_mask(const lbm_params* p, lbm_lattice_info* out) {
@@ -771,6 +894,7 @@ int lbm_load(lbm_handle* h, const char* path) {
     LBM_CK(cudaMemcpy(h->d_info, info.data(), h->N * sizeof(lbm_lattice_info), cudaMemcpyHostToDevice));
     LBM_CK(cudaMemcpy(h->d_macro, macro.data(), 3 * h->N * sizeof(float), cudaMemcpyHostToDevice));
     h->host_info = hinfo;
+    h->host_mirror_valid = false;
     h->cur = hd.cur & 1;
     h->tau = hd.tau;
     h->omega = 1.0f / hd.tau;

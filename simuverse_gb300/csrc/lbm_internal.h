@@ -34,6 +34,11 @@ struct lbm_handle {
     bool stepped_since_init = false;  // macro_tex holds (0,0,0,1) right after init
     float pre_x = 0.0f, pre_y = 0.0f;  // FluidSimulator::pre_pos
     int device = 0;
+    // device copy of host_info for batched edits (lbm_apply_edits); uploaded on first use
+    lbm_lattice_info* d_host_info = nullptr;
+    bool host_mirror_valid = false;
+    void* d_edits = nullptr;  // edit lists of lbm_apply_edits
+    size_t edits_cap = 0;
 };
 
 namespace lbm {
@@ -65,6 +70,18 @@ cudaError_t launch_count_nonfinite(lbm_handle* h, cudaStream_t s);
 cudaError_t launch_conservation_f32_phys(const float* A, const uint16_t* flags, size_t N, double* part, double* out,
                                          cudaStream_t s);
 cudaError_t launch_macro_error(lbm_handle* h, lbm_handle* ref, double* d_out4, cudaStream_t s);
+// batched interactive edits (lbm_kernels.cu): obstacles[j] = (x, y, seq), forces[k] =
+// (cell, seq, vx bits, vy bits); sequence numbers give the order of the edits
+struct EditObstacle {
+    int32_t x, y, seq, pad;
+};
+struct EditForce {
+    uint32_t cell;
+    int32_t seq;
+    float vx, vy;
+};
+cudaError_t launch_edits(lbm_handle* h, const EditObstacle* d_obst, int nobst, const EditForce* d_force, int nforce,
+                         int row0, int row1, cudaStream_t s);
 cudaError_t launch_macro_rgba16f(lbm_handle* h, uint16_t* d_rgba, cudaStream_t s);
 cudaError_t launch_to_absolute(lbm_handle* h, const void* state, void* dst, int dst_dtype, cudaStream_t s);
 cudaError_t launch_from_absolute(lbm_handle* h, const void* src, int src_dtype, void* state, cudaStream_t s);

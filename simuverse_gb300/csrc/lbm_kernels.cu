@@ -413,9 +413,85 @@ __global__ void k_from_absolute(const D* __restrict__ src, typename ST::T* __res
 }
 
 // ------------------------------------------------------------------------------------
+// batched interactive edits: the result of applying, in sequence order, obstacle discs
+// (d2q9_node.rs:215-245: the disc goes into the host copy of the mask and rows [y-28, y+28)
+// of that copy overwrite the device mask) and force-stroke cells (d2q9_node.rs:263-300: one
+// record per cell written to the device mask only).  For a cell of an obstacle row, the last
+// obstacle whose rows hold it decides its value: the obstacle record if a disc of that or an
+// earlier obstacle covers it, else the host copy; a force cell keeps its record unless a
+// later obstacle's rows hold it.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ bool in_obstacle_disc(int x, int y, int ox, int oy) {
+    // fluid/mod.rs:57-59 with the cell centres of d2q9_node.rs:222-229
+    const float px = __fsub_rn(__fadd_rn((float)x, 0.5f), __fadd_rn((float)ox, 0.5f));
+    const float py = __fsub_rn(__fadd_rn((float)y, 0.5f), __fadd_rn((float)oy, 0.5f));
+    return __fsqrt_rn(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py))) <= 28.0f;
+}
+
+__global__ void k_edit_obstacles(lbm_lattice_info* __restrict__ info, lbm_lattice_info* __restrict__ host_copy,
+                                 const EditObstacle* __restrict__ ob, int nobst, int nx, int row0) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = row0 + (int)blockIdx.y;
+    if (x >= nx) return;
+    int last = -1;
+    bool cover_any = false, cover_last = false;
+    for (int j = 0; j < nobst; ++j) {
+        const EditObstacle o = ob[j];
+        const bool row = y >= o.y - 28 && y < o.y + 28;
+        const bool disc = row && in_obstacle_disc(x, y, o.x, o.y);
+        cover_any |= disc;
+        if (row) {
+            last = j;
+            cover_last = cover_any;
+        }
+    }
+    if (last < 0) return;
+    const size_t c = (size_t)y * nx + x;
+    lbm_lattice_info obst;
+    obst.material = LBM_OBSTACLE;
+    obst.block_iter = -1;
+    obst.vx = 0.0f;
+    obst.vy = 0.0f;
+    const lbm_lattice_info orig = host_copy[c];
+    info[c] = cover_last ? obst : orig;
+    if (cover_any) host_copy[c] = obst;
+}
+
+__global__ void k_edit_forces(lbm_lattice_info* __restrict__ info, const EditObstacle* __restrict__ ob, int nobst,
+                              const EditForce* __restrict__ fc, int nforce, int nx) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nforce) return;
+    const EditForce f = fc[k];
+    const int y = (int)(f.cell / (uint32_t)nx);
+    for (int j = 0; j < nobst; ++j)
+        if (ob[j].seq > f.seq && y >= ob[j].y - 28 && y < ob[j].y + 28) return;
+    lbm_lattice_info r;
+    r.material = LBM_EXTERNAL_FORCE;
+    r.block_iter = 90;
+    r.vx = f.vx;
+    r.vy = f.vy;
+    info[f.cell] = r;
+}
+
+// ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
 static inline dim3 cell_grid(const lbm_handle* h) { return dim3((unsigned)((h->nx + TPB - 1) / TPB), (unsigned)h->ny); }
+
+cudaError_t launch_edits(lbm_handle* h, const EditObstacle* d_obst, int nobst, const EditForce* d_force, int nforce,
+                         int row0, int row1, cudaStream_t s) {
+    if (nobst > 0 && row1 > row0) {
+        k_edit_obstacles<<<dim3((unsigned)((h->nx + TPB - 1) / TPB), (unsigned)(row1 - row0)), TPB, 0, s>>>(
+            h->d_info, h->d_host_info, d_obst, nobst, h->nx, row0);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (nforce > 0) {
+        k_edit_forces<<<(nforce + 127) / 128, 128, 0, s>>>(h->d_info, d_obst, nobst, d_force, nforce, h->nx);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
 
 cudaError_t launch_build_flags(const lbm_handle* h, cudaStream_t s) {
     k_build_flags<<<cell_grid(h), TPB, 0, s>>>(h->d_info, h->d_flags, h->nx, h->ny, h->p.mode);

@@ -62,6 +62,7 @@ class FluidSimulator:
         self.nx, self.ny = int(nx), int(ny)
         self.N = self.nx * self.ny
         self.mode, self.dtype, self.scene = mode, dtype, scene
+        self.pixel_size = int(pixel_size)
 
     # ------------------------------------------------------------------ lifetime
     def close(self):
@@ -138,6 +139,19 @@ class FluidSimulator:
         info = np.ascontiguousarray(info, dtype=nat.INFO_DTYPE).reshape(self.ny, self.nx)
         nat.check(self._lib.lbm_set_info(self._h, nat.ptr(info)))
 
+    def apply_edits(self, edits) -> int:
+        """Batched interaction on the GPU (lbm_apply_edits): edits is a list of tuples
+        (kind, *args) with kind in obstacle (x, y), click (px, py), force (pos_x, pos_y, pre_x,
+        pre_y), touch_begin (), touch_move (px, py).  Returns the number of mask writes."""
+        arr = (nat.Edit * max(1, len(edits)))()
+        for i, e in enumerate(edits):
+            arr[i].kind = nat.EDITS[e[0]]
+            vals = list(e[1:]) + [0.0] * (4 - len(e[1:]))
+            arr[i].a, arr[i].b, arr[i].c, arr[i].d = (float(v) for v in vals)
+        n = ctypes.c_int32()
+        nat.check(self._lib.lbm_apply_edits(self._h, arr, len(edits), ctypes.byref(n)))
+        return n.value
+
     # ------------------------------------------------------------------ fields
     def read_macro(self):
         """(rho, ux, uy) of the last step as (ny, nx) float32 arrays."""
@@ -191,6 +205,10 @@ class FluidSimulator:
         if rc not in (nat.LBM_OK, nat.LBM_ERR_NAN):
             nat.check(rc)
         return int(n.value)
+
+    def sync(self):
+        """Wait for the handle's stream (lbm_status)."""
+        self.status()
 
     def status(self):
         """Raises LbmError(LBM_ERR_TIMEOUT) if a step kernel gave up on a bounded wait."""
