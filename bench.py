@@ -295,8 +295,9 @@ def run_gpu(args):
 
 def run_precision(args):
     """Precision form at 8192^2: GLUPS of FP32 / FP16 / BF16 storage with each kernel
-    variant, and the error of each against an FP64 run of the same channel after
-    args.steps steps (rel L2 of rho and u, FP64 mass drift)."""
+    variant, and the error of each against an FP64 run of the same channel at checkpoints up
+    to args.steps steps (rel L2 of rho and u; the open channel's mass change, for
+    comparison with FP64's)."""
     import torch
 
     from simuverse_gb300 import FluidSimulator
@@ -307,7 +308,7 @@ def run_precision(args):
     out = {"workload": "precision", "nx": nx, "ny": ny, "glups": {}, "errors": {}}
     base = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
                 seed=1234)
-    for dtype in ("f32", "f16", "bf16"):
+    for dtype in () if args.skip_glups else ("f32", "f16", "bf16"):
         for kernel in ("cell", "vec2", "vec4", "bulk"):
             sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel, **base)
             sim.set_stream(stream.cuda_stream)
@@ -321,22 +322,31 @@ def run_precision(args):
             g = nx * ny * args.timing_steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
             out["glups"]["%s/%s" % (dtype, kernel)] = g
             sim.close()
+    # error study: all four storage forms step in lockstep; errors against FP64 at every
+    # checkpoint.  BGK is unstable for this channel at tau 0.51 (FP64 included), so taus
+    # below 0.55 use the KBC collision for every form.
+    checkpoints = sorted(set([c for c in args.checkpoints if c < args.steps] + [args.steps]))
     for tau in args.taus:
-        ref = FluidSimulator(nx, ny, dtype="f64", tau=tau, **base)
-        m0 = ref.conservation()[0]
-        ref.step(args.steps)
-        m_ref = ref.conservation()[0]
-        row = {"fp64_mass_drift": (m_ref - m0) / m0}
-        for dtype in ("f32", "f16", "bf16"):
-            sim = FluidSimulator(nx, ny, dtype=dtype, tau=tau, **base)
-            s0 = sim.conservation()[0]
-            sim.step(args.steps)
-            err = sim.macro_error(ref)
-            row[dtype] = {"rel_l2_rho": err[0], "rel_l2_u": err[1], "max_du": err[2],
-                          "mass_drift": (sim.conservation()[0] - s0) / s0, "nonfinite": sim.nonfinite_count()}
-            sim.close()
-        ref.close()
-        out["errors"]["tau=%g" % tau] = row
+        coll = args.error_collision if args.error_collision != "auto" else ("kbc" if tau < 0.55 else "bgk")
+        sims = {d: FluidSimulator(nx, ny, dtype=d, tau=tau, collision=coll, **base) for d in ("f64", "f32", "f16", "bf16")}
+        m0 = {d: s.conservation()[0] for d, s in sims.items()}
+        rows, done = [], 0
+        for cp in checkpoints:
+            for s in sims.values():
+                s.step(cp - done)
+            done = cp
+            ref = sims["f64"]
+            row = {"step": cp, "fp64_mass_change": (ref.conservation()[0] - m0["f64"]) / m0["f64"],
+                   "fp64_nonfinite": ref.nonfinite_count()}
+            for d in ("f32", "f16", "bf16"):
+                err = sims[d].macro_error(ref)
+                row[d] = {"rel_l2_rho": err[0], "rel_l2_u": err[1], "max_du": err[2],
+                          "mass_change": (sims[d].conservation()[0] - m0[d]) / m0[d],
+                          "nonfinite": sims[d].nonfinite_count()}
+            rows.append(row)
+        for s in sims.values():
+            s.close()
+        out["errors"]["tau=%g" % tau] = {"collision": coll, "checkpoints": rows}
     out["steps"] = args.steps
     print(json.dumps(out), flush=True)
 
@@ -393,9 +403,11 @@ def run_closure(args):
     setup = TurbulenceSetup(nf=args.nx, factor=4, tau_f=0.5005, k_coarse=args.k_coarse, collision=args.collision)
     out = {"workload": "closure", "fine": args.nx, "coarse": setup.nc, "tau_f": setup.tau_f, "tau_c": setup.tau_c,
            "k_coarse": setup.k_coarse, "collision": args.collision}
-    c = Closure(setup.nc, setup.nc, seed=args.seed)
+    c = Closure(setup.nc, setup.nc, seed=args.seed, inputs=args.inputs, target=args.target, projection=args.projection)
+    out["form"] = {"inputs": args.inputs, "target": args.target, "projection": args.projection}
+    out["sources"] = list(args.sources)
     seeds = list(range(1000, 1000 + args.train_seeds))
-    npairs = args.train_seeds * args.snapshots * 2
+    npairs = args.train_seeds * args.snapshots * len(args.sources)
     curve = []
     out["datagen_s"] = 0.0
     out["train_s"] = 0.0
@@ -403,7 +415,8 @@ def run_closure(args):
         c.reserve(npairs + 64, 256, 8)
         t0 = time.perf_counter()
         generate_pairs(c, setup, seeds, snapshots=args.snapshots, interval=args.interval, crop=256,
-                       rng_seed=args.seed + rnd, corrected=c if rnd > 0 else None, calibrate=rnd == 0)
+                       rng_seed=args.seed + rnd, sources=tuple(args.sources), corrected=c if rnd > 0 else None,
+                       calibrate=rnd == 0)
         out["datagen_s"] += time.perf_counter() - t0
         hold = max(1, c.npairs // 20)
         if rnd == 0:
@@ -432,6 +445,89 @@ def run_closure(args):
     print(json.dumps(out), flush=True)
 
 
+def run_view(args):
+    """Consumers of the macro field on a physics channel of args.nx x args.ny cells drawn on
+    a canvas of 2 pixels per cell: the reference frame (two steps, each followed by a
+    particle update; then the canvas present), the curl field and the curl colour map.
+    Device time per operation (CUDA events on the lattice's stream), and the bandwidth of the
+    canvas-sized kernels against the HBM roofline (algorithmic bytes: present 12 B read +
+    16 B RGBA write + 4 B alpha write per lit pixel; curl 8 B read + 4 B write per cell;
+    colour map 16 B write per pixel + the field and curl planes once)."""
+    import numpy as np
+    import torch
+
+    from simuverse_gb300 import FluidSimulator
+    from simuverse_gb300 import _native as nat
+    from simuverse_gb300.view import Particles
+
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    nx, ny = args.nx, args.ny
+    sim = FluidSimulator(nx, ny, mode="physics", scene="channel", tau=0.56, inlet_speed=0.05, solid_fraction=0.05,
+                         seed=args.seed, pixel_size=2)
+    sim.set_stream(stream.cuda_stream)
+    ps = Particles(sim, count=args.particles, life_time=60.0, point_size=2, seed=1, color_ty=1)
+    cw, ch = ps.canvas_w, ps.canvas_h
+    out = {"workload": "view", "nx": nx, "ny": ny, "canvas": [cw, ch], "particles": ps.count}
+    lib = nat.load()
+    curl_buf = torch.empty(nx * ny, dtype=torch.float32, device="cuda")
+    rgba = torch.empty(cw * ch * 4, dtype=torch.float32, device="cuda")
+    import ctypes
+
+    def op_curl():
+        nat.check(lib.lbm_curl(sim.handle, ctypes.c_void_p(curl_buf.data_ptr())))
+
+    def op_colorize():
+        nat.check(lib.lbm_colorize(sim.handle, 0, ctypes.c_void_p(curl_buf.data_ptr()), cw, ch,
+                                   ctypes.c_void_p(rgba.data_ptr())))
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # warm the field and the canvas with a few frames
+    for _ in range(50):
+        ps.compute()
+        ps.present()
+    peak = measured_peak()[0]
+    ms = {}
+    ms["step"] = timed(lambda: sim.step(1), args.timing_steps // 10)
+    ms["particles_update"] = timed(ps.update, 200)
+    lit = float(np.mean(ps.canvas()[..., 0] > 0.001))
+    ms["present"] = timed(ps.present, 50)
+    ms["curl"] = timed(op_curl, 50)
+    ms["colorize"] = timed(op_colorize, 50)
+
+    def frame():
+        ps.compute()
+        ps.present()
+
+    ms["frame"] = timed(frame, 50)
+    out["ms"] = ms
+    out["lit_fraction"] = lit
+    npix = cw * ch
+    bytes_present = npix * (12 + 16) + lit * npix * 4
+    bytes_curl = nx * ny * 12
+    bytes_color = npix * 16 + nx * ny * 16
+    out["gb_per_s"] = {"present": bytes_present / (ms["present"] * 1e-3) / 1e9,
+                       "curl": bytes_curl / (ms["curl"] * 1e-3) / 1e9,
+                       "colorize": bytes_color / (ms["colorize"] * 1e-3) / 1e9}
+    out["roofline_frac"] = {k: v / peak for k, v in out["gb_per_s"].items()}
+    out["particles_per_s"] = ps.count / (ms["particles_update"] * 1e-3)
+    out["peak_gbs"] = peak
+    print(json.dumps(out), flush=True)
+    ps.close()
+    sim.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -443,11 +539,15 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2"])
-    ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch", "closure"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch", "closure", "view"])
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snapshots", type=int, default=125)
     ap.add_argument("--interval", type=int, default=160)
-    ap.add_argument("--dagger", type=int, default=1)
+    ap.add_argument("--dagger", type=int, default=0)
+    ap.add_argument("--inputs", default="eq", choices=["eq", "neq"])
+    ap.add_argument("--target", default="populations", choices=["momentum", "equilibrium", "populations"])
+    ap.add_argument("--projection", default="cell", choices=["domain", "cell"])
+    ap.add_argument("--sources", nargs="+", default=["fresh"], choices=["fresh", "rollout"])
     ap.add_argument("--k-coarse", type=int, default=4)
     ap.add_argument("--train-iters", type=int, default=3000)
     ap.add_argument("--train-blocks", type=int, default=10)
@@ -456,10 +556,14 @@ def main():
     ap.add_argument("--check-every", type=int, default=2000)
     ap.add_argument("--collision", default="kbc", choices=["bgk", "kbc", "mrt", "regularized"])
     ap.add_argument("--taus", type=float, nargs="*", default=[0.51, 0.6, 0.9])
+    ap.add_argument("--checkpoints", type=int, nargs="*", default=[1000, 5000])
+    ap.add_argument("--error-collision", default="auto", choices=["auto", "bgk", "kbc"])
+    ap.add_argument("--skip-glups", action="store_true")
     ap.add_argument("--timing-steps", type=int, default=500)
     ap.add_argument("--domains", type=int, default=256)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--loop-steps", type=int, default=200)
+    ap.add_argument("--particles", type=int, default=205000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -471,6 +575,8 @@ def main():
         run_batch(args)
     elif args.workload == "closure":
         run_closure(args)
+    elif args.workload == "view":
+        run_view(args)
     else:
         run_gpu(args)
 

@@ -382,12 +382,13 @@ int lbm_batch_counters(const lbm_batch* b, uint64_t* steps, uint64_t* launches);
 /* ---------------------------------------------------------------------------------
    Learned closure of a coarsened lattice -- no counterpart in the reference.  A
    three-layer 3x3 convolution (9 -> 32 -> 32 -> 9 channels; BF16 weights and activations,
-   FP32 accumulation on the tensor cores) maps s_in * f_neq of every coarse cell to a
-   correction delta = P(y) / s_out of its populations; P removes the density and momentum
-   of the correction, so no cell's rho or j changes.  Trained on the GPU (own forward,
+   FP32 accumulation on the tensor cores) maps 9 input channels of every coarse cell
+   (lbm_closure_set_form) to a correction delta = P(y) / s_out of its populations; the
+   projection P removes the density and momentum of the correction, per cell or as field
+   means, so that the lattice's mass and momentum do not change.  Trained on the GPU (own forward,
    backward and Adam kernels) on pairs (coarse state C after k coarse steps from a
    coarse-grained fine state, coarse-grained fine state C* k * factor fine steps later),
-   target s_out * P(C* - C), loss over the interior of square crops.  Closure lattices
+   mean squared error against the target over the interior of square crops.  Closure lattices
    are physics-mode FP32 handles of the closure's size.
    --------------------------------------------------------------------------------- */
 typedef struct lbm_closure lbm_closure;
@@ -399,6 +400,22 @@ int lbm_closure_param_count(void);
 int lbm_closure_create(int32_t nx, int32_t ny, uint64_t seed, lbm_closure** out);
 int lbm_closure_destroy(lbm_closure* c);
 int lbm_closure_set_scales(lbm_closure* c, float s_in, float s_out);
+/* the form of the closure (defaults: NEQ, POPULATIONS, CELL).  Inputs: s_in * f_neq of each
+   cell, or s_in * (f_eq(rho, u) - w), which depends on the density and velocity fields only.
+   Target of a pair (pred, target): s_out * (target - pred), s_out * (deq(rho*, u*) -
+   deq(rho, u)), the difference of the equilibrium parts, or s_out * 3 w_i e_i . (j* - j),
+   the momentum difference alone.  Projection: P cell by cell
+   (no cell's density or momentum changes), or the field means of the output's density and
+   momentum removed (the total mass and momentum of the lattice do not change, a cell's
+   momentum may) */
+#define LBM_CLOSURE_INPUT_NEQ 0
+#define LBM_CLOSURE_INPUT_EQ 1
+#define LBM_CLOSURE_TARGET_POPULATIONS 0
+#define LBM_CLOSURE_TARGET_EQUILIBRIUM 1
+#define LBM_CLOSURE_TARGET_MOMENTUM 2
+#define LBM_CLOSURE_PROJECT_CELL 0
+#define LBM_CLOSURE_PROJECT_DOMAIN 1
+int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t projection);
 int lbm_closure_get_params(lbm_closure* c, float* out);
 int lbm_closure_set_params(lbm_closure* c, const float* in);
 /* coarse = block average over factor x factor cells of the fine lattice's density and

@@ -79,18 +79,27 @@ def project_t(g):
     return g - a - 3.0 * (EX * ax + EY * ay)
 
 
-def loss_and_grad(x0, T, params, emulate_bf16=True):
-    """Mean loss over the interior [3, S-3)^2 and the logical gradient vector."""
+def project_domain(y):
+    """Field means of the output's density and momentum removed (y: (..., H, W, 9))."""
+    m = y.sum(-1).mean(axis=(-2, -1))[..., None, None, None]
+    jx = (y * EX).sum(-1).mean(axis=(-2, -1))[..., None, None, None]
+    jy = (y * EY).sum(-1).mean(axis=(-2, -1))[..., None, None, None]
+    return y - W9 * (m + 3.0 * (EX * jx + EY * jy))
+
+
+def loss_and_grad(x0, T, params, emulate_bf16=True, project_cell=True):
+    """Mean loss over the interior [3, S-3)^2 and the logical gradient vector; the loss
+    compares P(y) (project_cell) or y with T."""
     W1, b1, W2, b2, W3, b3 = unpack(params)
     x0, x1, x2, y = forward(x0, params, False, emulate_bf16)
     n, H, W, _ = y.shape
     m = np.zeros((n, H, W, 1))
     m[:, 3:H - 3, 3:W - 3] = 1.0
     T = bf16(T) if emulate_bf16 else T
-    e = (project(y) - T) * m
+    e = ((project(y) if project_cell else y) - T) * m
     count = n * (H - 6) * (W - 6) * 9
     loss = float((e * e).sum() / count)
-    gy = project_t(2.0 * e / count) * m
+    gy = (project_t(2.0 * e / count) if project_cell else 2.0 * e / count) * m
 
     def dweights(x, g):
         dW = np.stack([shift(x, t // 3 - 1, t % 3 - 1, False).reshape(-1, x.shape[-1]).T @ g.reshape(-1, g.shape[-1])

@@ -20,7 +20,12 @@ def coarsen(fine, coarse, factor: int, neq_scale: float):
 
 
 class Closure:
-    def __init__(self, nx: int, ny: int, seed: int = 0, s_in: float = 1000.0, s_out: float = 1000.0):
+    INPUTS = {"neq": 0, "eq": 1}
+    TARGETS = {"populations": 0, "equilibrium": 1, "momentum": 2}
+    PROJECTIONS = {"cell": 0, "domain": 1}
+
+    def __init__(self, nx: int, ny: int, seed: int = 0, s_in: float = 1000.0, s_out: float = 1000.0,
+                 inputs: str = "neq", target: str = "populations", projection: str = "cell"):
         lib = nat.load()
         h = ctypes.c_void_p()
         nat.check(lib.lbm_closure_create(int(nx), int(ny), int(seed), ctypes.byref(h)))
@@ -28,6 +33,7 @@ class Closure:
         self.nx, self.ny = int(nx), int(ny)
         self.nparams = lib.lbm_closure_param_count()
         self.set_scales(s_in, s_out)
+        self.set_form(inputs, target, projection)
         self.crop = None
 
     def close(self):
@@ -44,6 +50,14 @@ class Closure:
     def set_scales(self, s_in: float, s_out: float):
         nat.check(self._lib.lbm_closure_set_scales(self._h, float(s_in), float(s_out)))
         self.s_in, self.s_out = float(s_in), float(s_out)
+
+    def set_form(self, inputs: str = "neq", target: str = "populations", projection: str = "cell"):
+        """inputs 'neq' (s_in * f_neq) or 'eq' (s_in * (f_eq(rho, u) - w)); target
+        'populations' (target - pred) or 'equilibrium' (difference of the equilibrium parts);
+        projection 'cell' (no cell's rho or j changes) or 'domain' (the lattice's totals do not)."""
+        nat.check(self._lib.lbm_closure_set_form(self._h, self.INPUTS[inputs], self.TARGETS[target],
+                                                 self.PROJECTIONS[projection]))
+        self.inputs, self.target, self.projection = inputs, target, projection
 
     @property
     def params(self) -> np.ndarray:
@@ -193,8 +207,17 @@ def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256,
                 fp = pred.read_populations(np.float64)
                 ft = target.read_populations(np.float64)
                 neq = _neq_and_momentum(fp)[0]
-                tgt = _project(ft - fp)
-                closure.set_scales(1.0 / max(float(neq.std()), 1e-12), 1.0 / max(float(tgt.std()), 1e-12))
+                feat = neq if closure.inputs == "neq" else (fp - _W9[:, None, None]) - neq
+                if closure.target == "equilibrium":
+                    tgt = (ft - _neq_and_momentum(ft)[0]) - (fp - neq)
+                elif closure.target == "momentum":
+                    dj = ((ft - fp) * _EX[:, None, None]).sum(0), ((ft - fp) * _EY[:, None, None]).sum(0)
+                    tgt = 3.0 * _W9[:, None, None] * (_EX[:, None, None] * dj[0] + _EY[:, None, None] * dj[1])
+                else:
+                    tgt = ft - fp
+                if closure.projection == "cell":
+                    tgt = _project(tgt)
+                closure.set_scales(1.0 / max(float(feat.std()), 1e-12), 1.0 / max(float(tgt.std()), 1e-12))
                 calibrated = True
             ox, oy = int(rng.integers(0, setup.nc)), int(rng.integers(0, setup.nc))
             if "fresh" in sources:
@@ -248,10 +271,11 @@ def evaluate(closure, setup, seed, fine_steps=20000, check_every=2000):
             closure.apply(corr)
         gx, gy = coarse_velocity_of(fine, setup.factor)
         norm = np.sqrt(np.sum(gx * gx + gy * gy))
-        row = {"fine_step": t, "fine_nonfinite": fine.nonfinite_count()}
+        row = {"fine_step": t, "fine_nonfinite": fine.nonfinite_count(), "ke_fine": float(0.5 * np.mean(gx * gx + gy * gy))}
         for name, s in (("plain", plain), ("closure", corr)):
             _, ux, uy = s.read_macro()
             row["err_" + name] = float(np.sqrt(np.sum((ux - gx) ** 2 + (uy - gy) ** 2)) / norm)
+            row["ke_" + name] = float(0.5 * np.mean(ux.astype(np.float64) ** 2 + uy.astype(np.float64) ** 2))
         rows.append(row)
     for s in (fine, plain, corr):
         s.close()

@@ -22,13 +22,13 @@ constexpr double MRT_S_E = 1.1, MRT_S_EPS = 1.0, MRT_S_Q = 1.2;
 template <class R, int COLL = LBM_COLLISION_BGK>
 __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size_t c, uint16_t* __restrict__ flags,
                                              lbm_lattice_info* __restrict__ info, R omega, R (&o)[9], R& rho_out,
-                                             R& ux_out, R& uy_out) {
+                                             R& ux_out, R& uy_out, const R U = R(1)) {
     const bool outlet = (m == LBM_OUTLET);
     if (m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
         const lbm_lattice_info in = info[c];
         const R ux = R(in.vx), uy = R(in.vy);
         const R S = d[0] + d[2] + d[4] + R(2) * (d[3] + d[6] + d[7]);
-        const R rho = (R(1) + S) / (R(1) - ux);
+        const R rho = (U + S) / (R(1) - ux);
         const R rux = rho * ux, ruy = rho * uy;
         d[1] = d[3] + (R(2) / R(3)) * rux;
         d[5] = d[7] + R(0.5) * (d[4] - d[2]) + rux / R(6) - R(0.5) * ruy;
@@ -36,14 +36,14 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
     }
     if (outlet) {  // zero-gradient outflow anchored at rho = 1: f_j <- f_j / rho
         const R dr = d[0] + d[1] + d[2] + d[3] + d[4] + d[5] + d[6] + d[7] + d[8];
-        const R inv = R(1) / (R(1) + dr);
+        const R inv = U / (U + dr);
 #pragma unroll
         for (int j = 0; j < 9; ++j) d[j] = (d[j] - PW<R>(j) * dr) * inv;
     }
     const R drho = d[0] + (((d[1] + d[3]) + (d[2] + d[4])) + ((d[5] + d[7]) + (d[6] + d[8])));
     R jx = (d[1] - d[3]) + ((d[5] - d[7]) + (d[8] - d[6]));
     R jy = (d[4] - d[2]) + ((d[7] - d[5]) + (d[8] - d[6]));
-    const R rho = R(1) + drho;
+    const R rho = U + drho;
     R Fx = R(0), Fy = R(0);
     const bool forced = (m == LBM_EXTERNAL_FORCE);
     if (forced) {  // Guo forcing with the reference's block_iter countdown
@@ -56,8 +56,8 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
             }
             info[c] = in;
         }
-        Fx = R(in.vx);
-        Fy = R(in.vy);
+        Fx = R(in.vx) * U;
+        Fy = R(in.vy) * U;
         jx = jx + R(0.5) * Fx;
         jy = jy + R(0.5) * Fy;
     }
@@ -103,7 +103,7 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
             const R dh = n[j] - ds[j];
-            const R inv_feq = recip_rn(PW<R>(j) + q[j]);
+            const R inv_feq = recip_rn(PW<R>(j) * U + q[j]);
             sh += ds[j] * dh * inv_feq;
             hh += dh * dh * inv_feq;
         }
@@ -221,7 +221,7 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
     // rest population from mass conservation: sum_j o_j = drho by construction (the BGK
     // value in exact arithmetic; removes the bias of the rounded weights' moments)
     o[0] = drho - (((o[1] + o[3]) + (o[2] + o[4])) + ((o[5] + o[7]) + (o[6] + o[8])));
-    rho_out = rho;
+    rho_out = rho * (R(1) / U);
     ux_out = ux;
     uy_out = uy;
 }
@@ -252,7 +252,7 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
         for (int j = 0; j < 9; ++j) {
             const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
             const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-            d[j] = ST::ld(A + (size_t)j * N + (row + (unsigned)sx));
+            d[j] = ST::ldu(A + (size_t)j * N + (row + (unsigned)sx));
         }
     } else {
 #pragma unroll
@@ -260,25 +260,25 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
             const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
             const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
             if (fl & (1u << (FL_DIR_SHIFT + j))) {
-                R v = ST::ld(A + (size_t)INV(j) * N + c);  // half-way bounce-back
+                R v = ST::ldu(A + (size_t)INV(j) * N + c);  // half-way bounce-back
                 if (fl & FL_MOVING) {
                     const lbm_lattice_info si = info[row + sx];
                     const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
                     // rounded product, not an FMA: a contracted wall term leaves a
                     // systematic mass drift of ~1e-12 per step in FP32
-                    if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j), uw));
+                    if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j) * R(ST::UNIT), uw));
                 }
                 d[j] = v;
             } else {
-                d[j] = ST::ld(A + (size_t)j * N + (row + (unsigned)sx));
+                d[j] = ST::ldu(A + (size_t)j * N + (row + (unsigned)sx));
             }
         }
     }
     R o[9], rho, ux, uy;
-    phys_collide<R, COLL>(d, m, fl, c, flags, info, omega, o, rho, ux, uy);
+    phys_collide<R, COLL>(d, m, fl, c, flags, info, omega, o, rho, ux, uy, R(ST::UNIT));
     if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
 #pragma unroll
-    for (int j = 0; j < 9; ++j) ST::st(B + (size_t)j * N + c, o[j]);
+    for (int j = 0; j < 9; ++j) ST::stu(B + (size_t)j * N + c, o[j]);
 }
 
 }  // namespace lbm

@@ -2,6 +2,8 @@
 // one thread, shared by the single-lattice kernel (lbm_step_vec.cu) and the batched persistent
 // kernel (lbm_batch.cu).
 //
+// Populations are loaded and stored in stored units (ST::ldu / ST::stu; FP16 keeps its 2^10
+// scale through the collision, which takes ST::UNIT as the unit density).
 // Cells x0..x0+CPT-1 (x0 a multiple of CPT) of row y; rows are `pitch` elements apart
 // (pitch % CPT == 0, pitch >= nx) and cells x >= nx are padding, never read by a fluid
 // cell.  Every population plane is read and written with one aligned vector access per
@@ -53,11 +55,11 @@ struct Vec4<StoreF16> {
         const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
         const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
         const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
-        r[0] = a.x * F16_INV_SCALE; r[1] = a.y * F16_INV_SCALE; r[2] = b.x * F16_INV_SCALE; r[3] = b.y * F16_INV_SCALE;
+        r[0] = a.x; r[1] = a.y; r[2] = b.x; r[3] = b.y;
     }
     __device__ __forceinline__ static void st(__half* p, const float (&r)[4]) {
-        const __half2 a = __floats2half2_rn(r[0] * F16_SCALE, r[1] * F16_SCALE);
-        const __half2 b = __floats2half2_rn(r[2] * F16_SCALE, r[3] * F16_SCALE);
+        const __half2 a = __floats2half2_rn(r[0], r[1]);
+        const __half2 b = __floats2half2_rn(r[2], r[3]);
         uint2 q;
         q.x = *reinterpret_cast<const unsigned*>(&a);
         q.y = *reinterpret_cast<const unsigned*>(&b);
@@ -110,10 +112,10 @@ struct Vec2<StoreF16> {
     __device__ __forceinline__ static void ld(const __half* p, float (&r)[2]) {
         const unsigned q = __ldg(reinterpret_cast<const unsigned*>(p));
         const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q));
-        r[0] = a.x * F16_INV_SCALE; r[1] = a.y * F16_INV_SCALE;
+        r[0] = a.x; r[1] = a.y;
     }
     __device__ __forceinline__ static void st(__half* p, const float (&r)[2]) {
-        const __half2 a = __floats2half2_rn(r[0] * F16_SCALE, r[1] * F16_SCALE);
+        const __half2 a = __floats2half2_rn(r[0], r[1]);
         *reinterpret_cast<unsigned*>(p) = *reinterpret_cast<const unsigned*>(&a);
     }
 };
@@ -180,19 +182,19 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             for (int k = 0; k < CPT; ++k) d[j][k] = v[k];
         } else if (EX(j) == 1) {  // source x - 1
             R prev = __shfl_up_sync(0xffffffffu, v[CPT - 1], 1);
-            if (own_left && active) prev = ST::ld(Aj + xl);
+            if (own_left && active) prev = ST::ldu(Aj + xl);
             d[j][0] = prev;
 #pragma unroll
             for (int k = 1; k < CPT; ++k) d[j][k] = v[k - 1];
         } else {  // source x + 1
             R next = __shfl_down_sync(0xffffffffu, v[0], 1);
-            if (own_right && active) next = ST::ld(Aj + xr);
+            if (own_right && active) next = ST::ldu(Aj + xr);
 #pragma unroll
             for (int k = 0; k < CPT - 1; ++k) d[j][k] = v[k + 1];
             d[j][CPT - 1] = next;
             if (x0 + CPT > nx && active) {  // row end inside this group: cell nx-1 wraps to 0
                 const int k = nx - 1 - x0;
-                d[j][k < 0 ? 0 : k] = ST::ld(Aj);
+                d[j][k < 0 ? 0 : k] = ST::ldu(Aj);
             }
         }
     }
@@ -215,15 +217,15 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             continue;
         }
         if (m == LBM_OUTLET) {  // zero-gradient: e_x = -1 populations come from the own column
-            dk[3] = ST::ld(A + 3 * N + r0 + x);
-            dk[6] = ST::ld(A + 6 * N + rp + x);
-            dk[7] = ST::ld(A + 7 * N + rm + x);
+            dk[3] = ST::ldu(A + 3 * N + r0 + x);
+            dk[6] = ST::ldu(A + 6 * N + rp + x);
+            dk[7] = ST::ldu(A + 7 * N + rm + x);
         }
         if (f & (0xFFu << (FL_DIR_SHIFT + 1))) {  // some pull source is solid: bounce back
 #pragma unroll
             for (int j = 1; j < 9; ++j) {
                 if (f & (1u << (FL_DIR_SHIFT + j))) {
-                    R v = ST::ld(A + c + (size_t)INV(j) * N);
+                    R v = ST::ldu(A + c + (size_t)INV(j) * N);
                     if (f & FL_MOVING) {
                         int sx = x - EX(j);
                         if (m == LBM_OUTLET && EX(j) == -1) sx = x;
@@ -231,14 +233,14 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
                         const size_t srow = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
                         const lbm_lattice_info si = info[srow + sx];
                         const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
-                        if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j), uw));
+                        if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j) * R(ST::UNIT), uw));
                     }
                     dk[j] = v;
                 }
             }
         }
         R o[9];
-        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k]);
+        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k], R(ST::UNIT));
 #pragma unroll
         for (int j = 0; j < 9; ++j) d[j][k] = o[j];
     }

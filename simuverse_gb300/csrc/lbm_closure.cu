@@ -3,7 +3,9 @@
 // and the conservation projection.  No counterpart in the reference.
 //
 // Features and outputs.  For a coarse cell with deviations d (= f - w), density rho and
-// velocity u, the input features are s_in * f_neq, f_neq = d - deq(rho, u) (9 channels).
+// velocity u, the input features are s_in * f_neq, f_neq = d - deq(rho, u), or (inputs
+// LBM_CLOSURE_INPUT_EQ) s_in * deq(rho, u), which depends on the macroscopic fields only
+// (9 channels either way).
 // The network output y (9 channels, output units) becomes the correction
 //   delta = P(y) / s_out,   P(y)_i = y_i - w_i (sum_k y_k + 3 e_i . sum_k e_k y_k),
 // which satisfies sum_i delta_i = 0 and sum_i e_i delta_i = 0 exactly (up to rounding):
@@ -93,15 +95,25 @@ __device__ __forceinline__ void non_equilibrium(float (&v)[9]) {
     }
 }
 
-// features of an H x W window at (ox, oy) of an nx x ny periodic coarse field
+// features of an H x W window at (ox, oy) of an nx x ny periodic coarse field: s_in * f_neq
+// (inputs LBM_CLOSURE_INPUT_NEQ) or s_in * deq(rho, u) (LBM_CLOSURE_INPUT_EQ)
 __global__ void k_features(const float* __restrict__ d, int nx, int ny, int ox, int oy, int H, int W, float s_in,
-                           __nv_bfloat16* __restrict__ out) {
+                           int inputs, __nv_bfloat16* __restrict__ out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= W) return;
     const int gx = (ox + x) % nx, gy = (oy + y) % ny;
     float v[9];
     load_dev(d, (size_t)nx * ny, (size_t)gy * nx + gx, v);
-    non_equilibrium(v);
+    if (inputs == LBM_CLOSURE_INPUT_EQ) {
+        float n[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) n[i] = v[i];
+        non_equilibrium(n);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] -= n[i];
+    } else {
+        non_equilibrium(v);
+    }
     unsigned* o = reinterpret_cast<unsigned*>(out + ((size_t)y * W + x) * 16);
 #pragma unroll
     for (int k = 0; k < 4; ++k) o[k] = pack_bf16x2(s_in * v[2 * k], s_in * v[2 * k + 1]);
@@ -109,16 +121,42 @@ __global__ void k_features(const float* __restrict__ d, int nx, int ny, int ox, 
     o[5] = o[6] = o[7] = 0u;
 }
 
-// target s_out * P(target - pred) of an H x W window at (ox, oy)
+// target of an H x W window at (ox, oy): s_out * (target - pred) (LBM_CLOSURE_TARGET_POPULATIONS),
+// s_out * (deq(rho*, u*) - deq(rho, u)) (LBM_CLOSURE_TARGET_EQUILIBRIUM) or the momentum
+// difference alone, s_out * 3 w_i e_i . (j* - j) (LBM_CLOSURE_TARGET_MOMENTUM); projected cell by
+// cell with P when the projection is LBM_CLOSURE_PROJECT_CELL
 __global__ void k_target(const float* __restrict__ dt, const float* __restrict__ dp, int nx, int ny, int ox, int oy,
-                         int H, int W, float s_out, __nv_bfloat16* __restrict__ out) {
+                         int H, int W, float s_out, int target, int project_cell, __nv_bfloat16* __restrict__ out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= W) return;
     const size_t N = (size_t)nx * ny, c = (size_t)((oy + y) % ny) * nx + (ox + x) % nx;
     float v[9];
+    if (target == LBM_CLOSURE_TARGET_MOMENTUM) {
+        float jx = 0.0f, jy = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) v[i] = dt[c + i * N] - dp[c + i * N];
-    project9(v);
+        for (int i = 0; i < 9; ++i) {
+            const float df = dt[c + i * N] - dp[c + i * N];
+            jx += (float)EX(i) * df;
+            jy += (float)EY(i) * df;
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = 3.0f * PW<float>(i) * ((float)EX(i) * jx + (float)EY(i) * jy);
+    } else if (target == LBM_CLOSURE_TARGET_EQUILIBRIUM) {
+        float a[9], b[9], na[9], nb[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            a[i] = na[i] = dt[c + i * N];
+            b[i] = nb[i] = dp[c + i * N];
+        }
+        non_equilibrium(na);
+        non_equilibrium(nb);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = (a[i] - na[i]) - (b[i] - nb[i]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v[i] = dt[c + i * N] - dp[c + i * N];
+    }
+    if (project_cell) project9(v);
     unsigned* o = reinterpret_cast<unsigned*>(out + ((size_t)y * W + x) * 16);
 #pragma unroll
     for (int k = 0; k < 4; ++k) o[k] = pack_bf16x2(s_out * v[2 * k], s_out * v[2 * k + 1]);
@@ -126,8 +164,56 @@ __global__ void k_target(const float* __restrict__ dt, const float* __restrict__
     o[5] = o[6] = o[7] = 0u;
 }
 
-// d += P(y) / s_out over a full nx x ny field (y: [ny][nx][16] f32)
-__global__ void k_apply(const float* __restrict__ y, float* __restrict__ d, int nx, int ny, float inv_s_out) {
+// FP64 partial sums over the field of (sum_i y_i, sum_i e_x y_i, sum_i e_y y_i), one triple
+// per block, grid-stride over cells in a fixed order
+__global__ void k_ysums(const float* __restrict__ y, size_t N, double* __restrict__ part) {
+    __shared__ double red[3][32];
+    double m = 0.0, jx = 0.0, jy = 0.0;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        float s = 0.0f, sx = 0.0f, sy = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const float v = y[c * 16 + i];
+            s += v;
+            sx += (float)EX(i) * v;
+            sy += (float)EY(i) * v;
+        }
+        m += s;
+        jx += sx;
+        jy += sy;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_down_sync(0xffffffffu, m, o);
+        jx += __shfl_down_sync(0xffffffffu, jx, o);
+        jy += __shfl_down_sync(0xffffffffu, jy, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = m;
+        red[1][threadIdx.x >> 5] = jx;
+        red[2][threadIdx.x >> 5] = jy;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+        part[3 * blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// means[k] = sum of the partials of component k / N, in block order
+__global__ void k_ymeans(const double* __restrict__ part, int nblocks, double inv_n, double* __restrict__ means) {
+    if (blockIdx.x != 0 || threadIdx.x >= 3) return;
+    double t = 0.0;
+    for (int b = 0; b < nblocks; ++b) t += part[3 * b + threadIdx.x];
+    means[threadIdx.x] = t * inv_n;
+}
+
+// the correction delta of a full nx x ny field (y: [ny][nx][16] f32): P(y) / s_out cell by
+// cell (means == nullptr), or (y_i - w_i (m + 3 e_i . j)) / s_out with (m, j) the field means
+// of the network output's density and momentum, so that the field's total mass and momentum
+// do not change.  accumulate: d += delta (the populations); else d = delta (9 planes)
+__global__ void k_apply(const float* __restrict__ y, float* __restrict__ d, int nx, int ny, float inv_s_out,
+                        const double* __restrict__ means, int accumulate) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
     if (x >= nx) return;
     const size_t N = (size_t)nx * ny, c = (size_t)r * nx + x;
@@ -136,15 +222,27 @@ __global__ void k_apply(const float* __restrict__ y, float* __restrict__ d, int 
     const float4 a = yp[0], b = yp[1];
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
     v[8] = y[c * 16 + 8];
-    project9(v);
+    if (means) {
+        const float m = (float)means[0], jx = (float)means[1], jy = (float)means[2];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) d[c + i * N] += inv_s_out * v[i];
+        for (int i = 0; i < 9; ++i) v[i] -= PW<float>(i) * (m + 3.0f * ((float)EX(i) * jx + (float)EY(i) * jy));
+    } else {
+        project9(v);
+    }
+    if (accumulate) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) d[c + i * N] += inv_s_out * v[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) d[c + i * N] = inv_s_out * v[i];
+    }
 }
 
 // loss over the interior [3, H-3) x [3, W-3) of every image and the output gradient
-// g = P^T(2 (P(y) - T) / count) (zero outside the interior); per-block FP64 loss partials
+// g = P^T(2 (P(y) - T) / count) (zero outside the interior), or without P when project_cell
+// is 0; per-block FP64 loss partials
 __global__ void k_loss(const float* __restrict__ y, const __nv_bfloat16* __restrict__ T, int nimg, int H, int W,
-                       float inv_count, __nv_bfloat16* __restrict__ g, double* __restrict__ part) {
+                       float inv_count, int project_cell, __nv_bfloat16* __restrict__ g, double* __restrict__ part) {
     __shared__ double red[32];
     const size_t total = (size_t)nimg * H * W;
     double acc = 0.0;
@@ -159,14 +257,14 @@ __global__ void k_loss(const float* __restrict__ y, const __nv_bfloat16* __restr
         float v[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) v[i] = y[c * 16 + i];
-        project9(v);
+        if (project_cell) project9(v);
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
             const float e = v[i] - __bfloat162float(T[c * 16 + i]);
             acc += (double)e * (double)e;
             v[i] = 2.0f * e * inv_count;
         }
-        project9_t(v);
+        if (project_cell) project9_t(v);
 #pragma unroll
         for (int k = 0; k < 4; ++k) go[k] = pack_bf16x2(v[2 * k], v[2 * k + 1]);
         go[4] = pack_bf16x2(v[8], 0.0f);
@@ -280,6 +378,10 @@ namespace cl = lbm::closure;
 struct lbm_closure {
     int nx = 0, ny = 0;
     float s_in = 1000.0f, s_out = 1000.0f;
+    int inputs = LBM_CLOSURE_INPUT_NEQ;
+    int target = LBM_CLOSURE_TARGET_POPULATIONS;
+    int projection = LBM_CLOSURE_PROJECT_CELL;
+    double* dmeans = nullptr;  // reduction partials (RED_BLOCKS x 3) and the 3 field means
     int device = 0;
     cudaStream_t stream = nullptr;
     float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr, *mask = nullptr;
@@ -398,8 +500,8 @@ int loss_and_grad(lbm_closure* c, int nimg) {
     const int S = c->crop;
     C_TRY(forward<false>(c, c->bx0, c->bx1, c->bx2, c->by, nimg, S, S));
     const double count = (double)nimg * (S - 6) * (S - 6) * 9.0;
-    cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, nimg, S, S, (float)(1.0 / count), c->bg3,
-                                                         c->lpart);
+    cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, nimg, S, S, (float)(1.0 / count),
+                                                         c->projection == LBM_CLOSURE_PROJECT_CELL, c->bg3, c->lpart);
     C_CK(cudaGetLastError());
     cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
     C_CK(cudaGetLastError());
@@ -462,6 +564,7 @@ int lbm_closure_create(int32_t nx, int32_t ny, uint64_t seed, lbm_closure** out)
     if (e == cudaSuccess) e = dalloc(&c->x2, N * 32);
     if (e == cudaSuccess) e = dalloc(&c->y, N * 16);
     if (e == cudaSuccess) e = dalloc(&c->lpart, lbm::RED_BLOCKS);
+    if (e == cudaSuccess) e = dalloc(&c->dmeans, (size_t)lbm::RED_BLOCKS * 3 + 3);
     if (e == cudaSuccess) e = dalloc(&c->dloss, 8);
     if (e == cudaSuccess) e = dalloc(&c->dwpart, (size_t)cl::DW_BLOCKS * (9 * 32 * 32 + 32));
     if (e != cudaSuccess) {
@@ -504,7 +607,7 @@ int lbm_closure_destroy(lbm_closure* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->p,  c->g,  c->m,   c->v,   c->mask, c->wf1, c->wf2, c->wf3, c->wb3, c->wb2, c->x0,
                     c->x1, c->x2, c->y,   c->dsx, c->dst,  c->bx0, c->bt,  c->bx1, c->bx2, c->bg3, c->bg2,
-                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss};
+                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans};
     for (void* b : bufs) cudaFree(b);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -516,6 +619,21 @@ int lbm_closure_set_scales(lbm_closure* c, float s_in, float s_out) {
     if (!(s_in > 0.0f) || !(s_out > 0.0f)) return cfail(LBM_ERR_ARG, "scales must be positive");
     c->s_in = s_in;
     c->s_out = s_out;
+    return LBM_OK;
+}
+
+int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t projection) {
+    C_TRY(check_closure(c));
+    if (inputs != LBM_CLOSURE_INPUT_NEQ && inputs != LBM_CLOSURE_INPUT_EQ)
+        return cfail(LBM_ERR_ARG, "unknown closure input mode %d", inputs);
+    if (target != LBM_CLOSURE_TARGET_POPULATIONS && target != LBM_CLOSURE_TARGET_EQUILIBRIUM &&
+        target != LBM_CLOSURE_TARGET_MOMENTUM)
+        return cfail(LBM_ERR_ARG, "unknown closure target %d", target);
+    if (projection != LBM_CLOSURE_PROJECT_CELL && projection != LBM_CLOSURE_PROJECT_DOMAIN)
+        return cfail(LBM_ERR_ARG, "unknown closure projection %d", projection);
+    c->inputs = inputs;
+    c->target = target;
+    c->projection = projection;
     return LBM_OK;
 }
 
@@ -563,26 +681,52 @@ int lbm_coarsen(lbm_handle* fine, lbm_handle* coarse, int32_t factor, float neq_
     return LBM_OK;
 }
 
-int lbm_closure_apply(lbm_closure* c, lbm_handle* h) {
-    C_TRY(check_closure(c));
-    C_TRY(check_coarse(c, h));
-    C_CK(cudaSetDevice(c->device));
+}  // extern "C"
+
+namespace {
+
+// features, forward and the projected correction of the whole lattice h on h's stream:
+// added to h's populations (accumulate) or written to the 9 planes at out
+int correction(lbm_closure* c, lbm_handle* h, float* out, int accumulate) {
     cudaStream_t s = h->stream;
     cudaStream_t keep = c->stream;
     c->stream = s;  // run on the lattice's stream
     const dim3 g1((unsigned)((c->nx + 127) / 128), (unsigned)c->ny);
-    cl::k_features<<<g1, 128, 0, s>>>((const float*)h->buf[h->cur], c->nx, c->ny, 0, 0, c->ny, c->nx, c->s_in, c->x0);
+    cl::k_features<<<g1, 128, 0, s>>>((const float*)h->buf[h->cur], c->nx, c->ny, 0, 0, c->ny, c->nx, c->s_in,
+                                      c->inputs, c->x0);
     cudaError_t e = cudaGetLastError();
     int r = e == cudaSuccess ? forward<true>(c, c->x0, c->x1, c->x2, c->y, 1, c->ny, c->nx)
                              : cfail(LBM_ERR_CUDA, "features: %s", cudaGetErrorString(e));
+    const double* means = nullptr;
+    if (r == LBM_OK && c->projection == LBM_CLOSURE_PROJECT_DOMAIN) {
+        const size_t N = (size_t)c->nx * c->ny;
+        cl::k_ysums<<<lbm::RED_BLOCKS, 256, 0, s>>>(c->y, N, c->dmeans);
+        cl::k_ymeans<<<1, 32, 0, s>>>(c->dmeans, lbm::RED_BLOCKS, 1.0 / (double)N, c->dmeans + 3 * lbm::RED_BLOCKS);
+        means = c->dmeans + 3 * lbm::RED_BLOCKS;
+        c->launches += 2;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "field means: %s", cudaGetErrorString(e));
+    }
     if (r == LBM_OK) {
-        cl::k_apply<<<g1, 128, 0, s>>>(c->y, (float*)h->buf[h->cur], c->nx, c->ny, 1.0f / c->s_out);
+        cl::k_apply<<<g1, 128, 0, s>>>(c->y, out, c->nx, c->ny, 1.0f / c->s_out, means, accumulate);
         e = cudaGetLastError();
         if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "apply: %s", cudaGetErrorString(e));
     }
     c->stream = keep;
     c->launches += 2;
-    h->launches += 5;
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_closure_apply(lbm_closure* c, lbm_handle* h) {
+    C_TRY(check_closure(c));
+    C_TRY(check_coarse(c, h));
+    C_CK(cudaSetDevice(c->device));
+    const int r = correction(c, h, (float*)h->buf[h->cur], 1);
+    h->launches += c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 7 : 5;
     return r;
 }
 
@@ -632,9 +776,10 @@ int lbm_closure_add_pair(lbm_closure* c, lbm_handle* pred, lbm_handle* target, i
     const dim3 g((unsigned)((S + 127) / 128), (unsigned)S);
     const int x = ((ox % pred->nx) + pred->nx) % pred->nx, y = ((oy % pred->ny) + pred->ny) % pred->ny;
     cl::k_features<<<g, 128, 0, c->stream>>>((const float*)pred->buf[pred->cur], pred->nx, pred->ny, x, y, S, S,
-                                             c->s_in, c->dsx + off);
+                                             c->s_in, c->inputs, c->dsx + off);
     cl::k_target<<<g, 128, 0, c->stream>>>((const float*)target->buf[target->cur], (const float*)pred->buf[pred->cur],
-                                           pred->nx, pred->ny, x, y, S, S, c->s_out, c->dst + off);
+                                           pred->nx, pred->ny, x, y, S, S, c->s_out, c->target,
+                                           c->projection == LBM_CLOSURE_PROJECT_CELL, c->dst + off);
     C_CK(cudaGetLastError());
     c->launches += 2;
     ++c->npairs;
@@ -695,7 +840,8 @@ int lbm_closure_eval(lbm_closure* c, int32_t begin, int32_t end, double* loss_ou
         C_CK(cudaMemcpyAsync(c->bt, c->dst + k0 * img, B * img * 2, cudaMemcpyDeviceToDevice, c->stream));
         C_TRY(forward<false>(c, c->bx0, c->bx1, c->bx2, c->by, B, S, S));
         const double count = (double)B * (S - 6) * (S - 6) * 9.0;
-        cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, B, S, S, (float)(1.0 / count), c->bg3,
+        cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, B, S, S, (float)(1.0 / count),
+                                                             c->projection == LBM_CLOSURE_PROJECT_CELL, c->bg3,
                                                              c->lpart);
         cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
         C_CK(cudaGetLastError());
@@ -740,38 +886,25 @@ int lbm_closure_loss_grad(lbm_closure* c, int32_t nimg, int32_t size, const floa
     return LBM_OK;
 }
 
-// network output P(y) / s_out (the correction delta, 9 channels per cell) of the whole
+// the correction delta (9 planes of nx * ny floats) the closure would add to the whole
 // lattice h, without applying it (inspection and tests)
 int lbm_closure_predict(lbm_closure* c, lbm_handle* h, float* delta_out) {
     C_TRY(check_closure(c));
     C_TRY(check_coarse(c, h));
     if (!delta_out) return cfail(LBM_ERR_ARG, "null output");
     C_CK(cudaSetDevice(c->device));
-    C_CK(cudaStreamSynchronize(h->stream));
-    const dim3 g1((unsigned)((c->nx + 127) / 128), (unsigned)c->ny);
-    cl::k_features<<<g1, 128, 0, c->stream>>>((const float*)h->buf[h->cur], c->nx, c->ny, 0, 0, c->ny, c->nx, c->s_in,
-                                              c->x0);
-    C_CK(cudaGetLastError());
-    C_TRY(forward<true>(c, c->x0, c->x1, c->x2, c->y, 1, c->ny, c->nx));
     const size_t N = (size_t)c->nx * c->ny;
-    std::vector<float> hy(N * 16);
-    C_CK(cudaMemcpyAsync(hy.data(), c->y, N * 16 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    C_CK(cudaStreamSynchronize(c->stream));
-    for (size_t i = 0; i < N; ++i) {
-        float v[9];
-        float s = 0.0f, sx = 0.0f, sy = 0.0f;
-        for (int k = 0; k < 9; ++k) {
-            v[k] = hy[i * 16 + k];
-            s += v[k];
-            sx += (float)lbm::EX(k) * v[k];
-            sy += (float)lbm::EY(k) * v[k];
-        }
-        for (int k = 0; k < 9; ++k) {
-            const float w = lbm::PW<float>(k);
-            delta_out[(size_t)k * N + i] = (v[k] - w * (s + 3.0f * ((float)lbm::EX(k) * sx + (float)lbm::EY(k) * sy))) / c->s_out;
-        }
+    float* d = nullptr;
+    C_CK(cudaMalloc((void**)&d, 9 * N * sizeof(float)));
+    int r = correction(c, h, d, 0);
+    if (r == LBM_OK) {
+        cudaError_t e = cudaMemcpyAsync(delta_out, d, 9 * N * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "predict: %s", cudaGetErrorString(e));
     }
-    return LBM_OK;
+    cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    return r;
 }
 
 int lbm_closure_counters(const lbm_closure* c, uint64_t* launches, uint64_t* adam_steps) {

@@ -63,8 +63,11 @@ struct StoreF32 {
     using T = float;
     using R = float;
     static constexpr int dtype = LBM_DTYPE_F32;
+    static constexpr float UNIT = 1.0f;
     __device__ __forceinline__ static R ld(const T* p) { return __ldg(p); }
     __device__ __forceinline__ static void st(T* p, R v) { *p = v; }
+    __device__ __forceinline__ static R ldu(const T* p) { return __ldg(p); }
+    __device__ __forceinline__ static void stu(T* p, R v) { *p = v; }
     __host__ __device__ static R to_r(T v) { return v; }
     __host__ __device__ static T from_r(R v) { return v; }
 };
@@ -72,8 +75,11 @@ struct StoreF64 {
     using T = double;
     using R = double;
     static constexpr int dtype = LBM_DTYPE_F64;
+    static constexpr double UNIT = 1.0;
     __device__ __forceinline__ static R ld(const T* p) { return __ldg(p); }
     __device__ __forceinline__ static void st(T* p, R v) { *p = v; }
+    __device__ __forceinline__ static R ldu(const T* p) { return __ldg(p); }
+    __device__ __forceinline__ static void stu(T* p, R v) { *p = v; }
     __host__ __device__ static R to_r(T v) { return v; }
     __host__ __device__ static T from_r(R v) { return v; }
 };
@@ -83,8 +89,13 @@ struct StoreF16 {
     using T = __half;
     using R = float;
     static constexpr int dtype = LBM_DTYPE_F16;
+    // the step kernels compute in stored units (deviations times 2^10): UNIT is the stored
+    // value of a unit density, ldu / stu move stored values without rescaling
+    static constexpr float UNIT = F16_SCALE;
     __device__ __forceinline__ static R ld(const T* p) { return __half2float(__ldg(p)) * F16_INV_SCALE; }
     __device__ __forceinline__ static void st(T* p, R v) { *p = __float2half_rn(v * F16_SCALE); }
+    __device__ __forceinline__ static R ldu(const T* p) { return __half2float(__ldg(p)); }
+    __device__ __forceinline__ static void stu(T* p, R v) { *p = __float2half_rn(v); }
     __host__ __device__ static R to_r(T v) { return __half2float(v) * F16_INV_SCALE; }
     __host__ __device__ static T from_r(R v) { return __float2half_rn(v * F16_SCALE); }
 };
@@ -92,8 +103,11 @@ struct StoreBF16 {
     using T = __nv_bfloat16;
     using R = float;
     static constexpr int dtype = LBM_DTYPE_BF16;
+    static constexpr float UNIT = 1.0f;
     __device__ __forceinline__ static R ld(const T* p) { return __bfloat162float(__ldg(p)); }
     __device__ __forceinline__ static void st(T* p, R v) { *p = __float2bfloat16_rn(v); }
+    __device__ __forceinline__ static R ldu(const T* p) { return __bfloat162float(__ldg(p)); }
+    __device__ __forceinline__ static void stu(T* p, R v) { *p = __float2bfloat16_rn(v); }
     __host__ __device__ static R to_r(T v) { return __bfloat162float(v); }
     __host__ __device__ static T from_r(R v) { return __float2bfloat16_rn(v); }
 };

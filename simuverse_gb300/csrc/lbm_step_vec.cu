@@ -21,7 +21,9 @@ __global__ void __launch_bounds__(VEC_TPB) k_phys_step_v4(const typename ST::T* 
     phys_cells4_update<ST, MACRO>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
 }
 
-// two cells per thread: one 32-bit access per plane for FP16 / BF16
+// two cells per thread: one 32-bit access per plane for FP16 / BF16 (threads that walk
+// several rows, amortising the column set-up, measured slower: register spills at 48
+// registers, or lower occupancy at 64)
 template <class ST, bool MACRO>
 __global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_v2(const typename ST::T* __restrict__ A,
                                                               typename ST::T* __restrict__ B,

@@ -220,12 +220,18 @@ __global__ void k_present_canvas(float* __restrict__ canvas, float4* __restrict_
 // one past the edge) and left/top to 0; a texel load one past the edge returns the edge
 // texel (bounds-restricted load).  curl = R.y - L.y + T.x - B.x, stored as
 // curl * 3.5 + 0.5 in an rgba16float texel
+__device__ __forceinline__ float texel1(const Field& f, const float* plane, int u, int v) {
+    u = u < 0 ? 0 : (u > f.nx - 1 ? f.nx - 1 : u);
+    v = v < 0 ? 0 : (v > f.ny - 1 ? f.ny - 1 : v);
+    return f.zero ? 0.0f : h16(__ldg(plane + (size_t)v * f.nx + u));
+}
+
 __global__ void k_curl(Field f, float* __restrict__ out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= f.nx) return;
-    const float3 R = texel(f, x + 1 > f.nx ? f.nx : x + 1, y), L = texel(f, x - 1 < 0 ? 0 : x - 1, y);
-    const float3 T = texel(f, x, y - 1 < 0 ? 0 : y - 1), B = texel(f, x, y + 1 > f.ny ? f.ny : y + 1);
-    const float curl = sub_rn(add_rn(sub_rn(R.y, L.y), T.x), B.x);
+    const float Ry = texel1(f, f.uy, x + 1 > f.nx ? f.nx : x + 1, y), Ly = texel1(f, f.uy, x - 1 < 0 ? 0 : x - 1, y);
+    const float Tx = texel1(f, f.ux, x, y - 1 < 0 ? 0 : y - 1), Bx = texel1(f, f.ux, x, y + 1 > f.ny ? f.ny : y + 1);
+    const float curl = sub_rn(add_rn(sub_rn(Ry, Ly), Tx), Bx);
     out[(size_t)y * f.nx + x] = h16(add_rn(mul_rn(curl, 3.5f), 0.5f));
 }
 

@@ -31,40 +31,87 @@ def _turbulent_sim(nx, ny, seed, tau=0.55, steps=20):
     return s
 
 
-def test_forward_matches_fp64_restatement(gpu):
+FORMS = [("neq", "populations", "cell"), ("eq", "equilibrium", "domain")]
+
+
+@pytest.mark.parametrize("form", FORMS, ids=["-".join(f) for f in FORMS])
+def test_forward_matches_fp64_restatement(gpu, form):
+    inputs, target, projection = form
     nx, ny = 64, 48
     rng = np.random.default_rng(0)
-    c = Closure(nx, ny, seed=1, s_in=3000.0, s_out=500.0)
+    s_in = 3000.0 if inputs == "neq" else 20.0
+    c = Closure(nx, ny, seed=1, s_in=s_in, s_out=500.0, inputs=inputs, target=target, projection=projection)
     p = _random_params(c, rng)
     c.params = p
     sim = _turbulent_sim(nx, ny, 4)
     delta = c.predict(sim)
-    # features from the state: s_in * f_neq
     f = sim.read_populations(np.float64).transpose(1, 2, 0)  # (ny, nx, 9)
     rho = f.sum(-1, keepdims=True)
     ux = (f * ref.EX).sum(-1, keepdims=True) / rho
     uy = (f * ref.EY).sum(-1, keepdims=True) / rho
     eu = ref.EX * ux + ref.EY * uy
     feq = ref.W9 * rho * (1 + 3 * eu + 4.5 * eu * eu - 1.5 * (ux * ux + uy * uy))
-    x0 = (3000.0 * (f - feq))[None]
+    x0 = (s_in * ((f - feq) if inputs == "neq" else (feq - ref.W9)))[None]
     _, _, _, y = ref.forward(x0, c.params, periodic=True, emulate_bf16=True)
-    expect = (ref.project(y) / 500.0)[0].transpose(2, 0, 1)
+    proj = ref.project(y) if projection == "cell" else ref.project_domain(y)
+    expect = (proj / 500.0)[0].transpose(2, 0, 1)
     err = np.max(np.abs(delta - expect)) / np.max(np.abs(expect))
     assert err < 2e-2, err
-    # the correction conserves density and momentum cell by cell
-    assert np.max(np.abs(delta.sum(0))) < 1e-6 * np.max(np.abs(delta)) + 1e-12
-    assert np.max(np.abs((delta * ref.EX[:, None, None]).sum(0))) < 1e-6 * np.max(np.abs(delta)) + 1e-12
+    scale = 1e-6 * np.max(np.abs(delta)) + 1e-12
+    if projection == "cell":  # the correction conserves density and momentum cell by cell
+        assert np.max(np.abs(delta.sum(0))) < scale
+        assert np.max(np.abs((delta * ref.EX[:, None, None]).sum(0))) < scale
+    else:  # ... or over the field, while moving momentum between cells
+        assert abs(delta.sum()) < scale * delta[0].size
+        assert abs((delta * ref.EX[:, None, None]).sum()) < scale * delta[0].size
+        assert np.max(np.abs((delta * ref.EX[:, None, None]).sum(0))) > 100 * scale
 
 
-def test_gradients_match_fp64_restatement(gpu):
+@pytest.mark.parametrize("target", ["populations", "equilibrium", "momentum"])
+@pytest.mark.parametrize("projection", ["cell", "domain"])
+def test_targets_match_restatement(gpu, target, projection):
+    """With all parameters zero the network output is 0, so the loss of one pair is the
+    mean square of the stored target over the crop's interior."""
+    n, S, s_out = 128, 32, 2000.0
+    c = Closure(n, n, seed=5, s_out=s_out, inputs="eq", target=target, projection=projection)
+    c.params = np.zeros(c.nparams, np.float32)
+    c.reserve(2, S, 1)
+    a = _turbulent_sim(n, n, 8, steps=30)
+    b = _turbulent_sim(n, n, 8, steps=34)
+    c.add_pair(a, b, 100, 7)  # wraps around the periodic edge
+    fa = a.read_populations(np.float64).transpose(1, 2, 0)
+    fb = b.read_populations(np.float64).transpose(1, 2, 0)
+
+    def deq(f):
+        rho = f.sum(-1, keepdims=True)
+        ux = (f * ref.EX).sum(-1, keepdims=True) / rho
+        uy = (f * ref.EY).sum(-1, keepdims=True) / rho
+        eu = ref.EX * ux + ref.EY * uy
+        return ref.W9 * rho * (1 + 3 * eu + 4.5 * eu * eu - 1.5 * (ux * ux + uy * uy))
+
+    if target == "momentum":
+        dj = ((fb - fa) * ref.EX).sum(-1, keepdims=True), ((fb - fa) * ref.EY).sum(-1, keepdims=True)
+        t = 3.0 * ref.W9 * (ref.EX * dj[0] + ref.EY * dj[1])
+    else:
+        t = (fb - fa) if target == "populations" else (deq(fb) - deq(fa))
+    if projection == "cell":
+        t = ref.project(t)
+    t = np.roll(np.roll(s_out * t, -7, axis=0), -100, axis=1)[:S, :S]
+    expect = float(np.mean(ref.bf16(t[3:S - 3, 3:S - 3]) ** 2))
+    got = c.eval(0, 1)
+    assert abs(got - expect) <= 1e-3 * expect, (got, expect)
+
+
+@pytest.mark.parametrize("projection", ["cell", "domain"])
+def test_gradients_match_fp64_restatement(gpu, projection):
     rng = np.random.default_rng(1)
-    c = Closure(64, 64, seed=2)
+    c = Closure(64, 64, seed=2, projection=projection)
     c.params = _random_params(c, rng)
     c.reserve(4, 32, 2)
     feats = rng.standard_normal((2, 32, 32, 9))
     targets = 0.3 * rng.standard_normal((2, 32, 32, 9))
     loss, g = c.loss_grad(feats, targets)
-    loss_ref, g_ref = ref.loss_and_grad(feats, targets, c.params, emulate_bf16=True)
+    loss_ref, g_ref = ref.loss_and_grad(feats, targets, c.params, emulate_bf16=True, project_cell=projection == "cell")
     assert abs(loss - loss_ref) / loss_ref < 1e-2
     # per layer: relative L2 error and direction of the gradient
     off = 0
@@ -76,10 +123,13 @@ def test_gradients_match_fp64_restatement(gpu):
         assert rel < 5e-2 and cos > 0.998, (n, rel, cos)
 
 
-def test_apply_conserves_mass_and_momentum(gpu):
+@pytest.mark.parametrize("form", FORMS, ids=["-".join(f) for f in FORMS])
+def test_apply_conserves_mass_and_momentum(gpu, form):
+    inputs, target, projection = form
     nx, ny = 128, 64
     rng = np.random.default_rng(3)
-    c = Closure(nx, ny, seed=3, s_in=3000.0, s_out=200.0)
+    c = Closure(nx, ny, seed=3, s_in=3000.0 if inputs == "neq" else 20.0, s_out=200.0, inputs=inputs, target=target,
+                projection=projection)
     c.params = _random_params(c, rng)
     sim = _turbulent_sim(nx, ny, 5)
     before = np.array(sim.conservation())
