@@ -407,7 +407,7 @@ int lbm_closure_set_scales(lbm_closure* c, float s_in, float s_out);
    the momentum difference alone.  Projection: P cell by cell
    (no cell's density or momentum changes), or the field means of the output's density and
    momentum removed (the total mass and momentum of the lattice do not change, a cell's
-   momentum may) */
+   momentum may; a momentum target needs the field projection) */
 #define LBM_CLOSURE_INPUT_NEQ 0
 #define LBM_CLOSURE_INPUT_EQ 1
 #define LBM_CLOSURE_TARGET_POPULATIONS 0

@@ -463,7 +463,8 @@ int conv(lbm_closure* c, const __nv_bfloat16* in, void* out, const __nv_bfloat16
                                   (int)smem));
         attr = true;
     }
-    const dim3 grid((unsigned)((W + cl::CONV_CELLS - 1) / cl::CONV_CELLS), (unsigned)H, (unsigned)nimg);
+    const dim3 grid((unsigned)((W + cl::CONV_CELLS - 1) / cl::CONV_CELLS), (unsigned)((H + cl::CONV_ROWS - 1) / cl::CONV_ROWS),
+                    (unsigned)nimg);
     cl::k_conv3x3<CIN, COUT, EPI, PER><<<grid, 32 * cl::CONV_WARPS, smem, c->stream>>>(in, out, w, bias, mask, H, W);
     C_CK(cudaGetLastError());
     ++c->launches;
@@ -631,6 +632,8 @@ int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t
         return cfail(LBM_ERR_ARG, "unknown closure target %d", target);
     if (projection != LBM_CLOSURE_PROJECT_CELL && projection != LBM_CLOSURE_PROJECT_DOMAIN)
         return cfail(LBM_ERR_ARG, "unknown closure projection %d", projection);
+    if (target == LBM_CLOSURE_TARGET_MOMENTUM && projection == LBM_CLOSURE_PROJECT_CELL)
+        return cfail(LBM_ERR_ARG, "the per-cell projection removes a momentum target entirely");
     c->inputs = inputs;
     c->target = target;
     c->projection = projection;

@@ -24,6 +24,7 @@ namespace closure {
 
 constexpr int CONV_WARPS = 4;
 constexpr int CONV_CELLS = 16 * CONV_WARPS;  // cells of one row per block
+constexpr int CONV_ROWS = 8;                 // output rows per block (weights staged once)
 
 enum { EPI_BIAS_RELU = 0, EPI_BIAS_F32 = 1, EPI_MASK = 2 };
 
@@ -50,7 +51,9 @@ struct SmemStride {
 // for EPI_BIAS_F32), wk: [9][COUT][CIN] bf16, bias: [COUT] f32 (unused for EPI_MASK),
 // mask: [nimg][H][W][COUT] bf16 (EPI_MASK only: out = acc where mask > 0, else 0).
 // PERIODIC: coordinates wrap; otherwise cells outside the image read as zero.
-// Requires W % 16 == 0.  Grid: (ceil(W / 64), H, nimg), 128 threads.
+// A block computes CONV_ROWS rows of 64 cells: it stages the weights and the CONV_ROWS + 2
+// input rows once, then each warp runs its 16 cells down the rows.
+// Requires W % 16 == 0.  Grid: (ceil(W / 64), ceil(H / CONV_ROWS), nimg), 128 threads.
 template <int CIN, int COUT, int EPI, bool PERIODIC>
 __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16* __restrict__ in,
                                                              void* __restrict__ out,
@@ -59,23 +62,24 @@ __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16
                                                              const __nv_bfloat16* __restrict__ mask, int H, int W) {
     constexpr int CS = SmemStride<CIN>::WORDS;
     constexpr int ROWC = CONV_CELLS + 2;
+    constexpr int SR = CONV_ROWS + 2;  // staged input rows
     constexpr int NT = COUT / 8;
     extern __shared__ __align__(16) unsigned csm[];
-    unsigned* sin = csm;                     // [3][ROWC][CS]
-    unsigned* sw = csm + 3 * ROWC * CS;      // [9][COUT][CS]
+    unsigned* sin = csm;                     // [SR][ROWC][CS]
+    unsigned* sw = csm + SR * ROWC * CS;     // [9][COUT][CS]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int img = blockIdx.z, y = blockIdx.y, xs = blockIdx.x * CONV_CELLS;
+    const int img = blockIdx.z, y0 = blockIdx.y * CONV_ROWS, xs = blockIdx.x * CONV_CELLS;
     const size_t img_off = (size_t)img * H * W;
 
-    // stage the input rows y-1..y+1, columns xs-1 .. xs+64 (16-byte vectors)
+    // stage the input rows y0-1..y0+CONV_ROWS, columns xs-1 .. xs+64 (16-byte vectors)
     constexpr int VPC = CIN / 8;  // 16-byte vectors per cell
-    for (int i = tid; i < 3 * ROWC * VPC; i += 32 * CONV_WARPS) {
+    for (int i = tid; i < SR * ROWC * VPC; i += 32 * CONV_WARPS) {
         const int v = i % VPC, cell = (i / VPC) % ROWC, r = i / (VPC * ROWC);
-        int gy = y + r - 1, gx = xs + cell - 1;
+        int gy = y0 + r - 1, gx = xs + cell - 1;
         uint4 val = make_uint4(0u, 0u, 0u, 0u);
         bool ok = true;
-        if (PERIODIC) {
-            gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+        if (PERIODIC) {  // staged rows run from -1 to H + CONV_ROWS, which may exceed 2 H
+            gy = ((gy % H) + H) % H;
             gx = gx < 0 ? gx + W : (gx >= W ? gx - W : gx);
         } else {
             ok = gy >= 0 && gy < H && gx >= 0 && gx < W;
@@ -93,46 +97,51 @@ __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16
     const int x0 = xs + warp * 16;
     if (x0 >= W) return;
     const int g = lane >> 2, c = lane & 3;
-    float acc[NT][4];
+#pragma unroll 1
+    for (int r = 0; r < CONV_ROWS; ++r) {
+        const int y = y0 + r;
+        if (y >= H) break;
+        float acc[NT][4];
 #pragma unroll
-    for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
+        for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
 #pragma unroll
-    for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3, dx = tap % 3;  // smem row / column offsets (0..2)
-        const unsigned* ra = sin + (dy * ROWC + warp * 16 + g + dx) * CS;
-        const unsigned* rb = ra + 8 * CS;
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;  // staged row / column offsets (0..2)
+            const unsigned* ra = sin + ((r + dy) * ROWC + warp * 16 + g + dx) * CS;
+            const unsigned* rb = ra + 8 * CS;
 #pragma unroll
-        for (int kc = 0; kc < CIN / 16; ++kc) {
-            const unsigned a0 = ra[kc * 8 + c], a1 = rb[kc * 8 + c];
-            const unsigned a2 = ra[kc * 8 + c + 4], a3 = rb[kc * 8 + c + 4];
+            for (int kc = 0; kc < CIN / 16; ++kc) {
+                const unsigned a0 = ra[kc * 8 + c], a1 = rb[kc * 8 + c];
+                const unsigned a2 = ra[kc * 8 + c + 4], a3 = rb[kc * 8 + c + 4];
 #pragma unroll
-            for (int n = 0; n < NT; ++n) {
-                const unsigned* wb = sw + (tap * COUT + n * 8 + g) * CS + kc * 8 + c;
-                mma_bf16_16816(acc[n], a0, a1, a2, a3, wb[0], wb[4]);
+                for (int n = 0; n < NT; ++n) {
+                    const unsigned* wb = sw + (tap * COUT + n * 8 + g) * CS + kc * 8 + c;
+                    mma_bf16_16816(acc[n], a0, a1, a2, a3, wb[0], wb[4]);
+                }
             }
         }
-    }
-    // epilogue: thread holds rows g, g+8 (cells x0+g, x0+g+8) and columns n*8 + 2c, +1
-    const size_t cell0 = img_off + (size_t)y * W + x0 + g;
+        // epilogue: thread holds rows g, g+8 (cells x0+g, x0+g+8) and columns n*8 + 2c, +1
+        const size_t cell0 = img_off + (size_t)y * W + x0 + g;
 #pragma unroll
-    for (int n = 0; n < NT; ++n) {
-        const int ch = n * 8 + 2 * c;
+        for (int n = 0; n < NT; ++n) {
+            const int ch = n * 8 + 2 * c;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const size_t cell = cell0 + 8 * h;
-            float v0 = acc[n][2 * h], v1 = acc[n][2 * h + 1];
-            if (EPI == EPI_BIAS_RELU) {
-                v0 = fmaxf(v0 + bias[ch], 0.0f);
-                v1 = fmaxf(v1 + bias[ch + 1], 0.0f);
-                reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
-            } else if (EPI == EPI_BIAS_F32) {
-                *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + cell * COUT + ch) =
-                    make_float2(v0 + bias[ch], v1 + bias[ch + 1]);
-            } else {
-                const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask + cell * COUT + ch);
-                v0 = __bfloat162float(mk.x) > 0.0f ? v0 : 0.0f;
-                v1 = __bfloat162float(mk.y) > 0.0f ? v1 : 0.0f;
-                reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+            for (int h = 0; h < 2; ++h) {
+                const size_t cell = cell0 + 8 * h;
+                float v0 = acc[n][2 * h], v1 = acc[n][2 * h + 1];
+                if (EPI == EPI_BIAS_RELU) {
+                    v0 = fmaxf(v0 + bias[ch], 0.0f);
+                    v1 = fmaxf(v1 + bias[ch + 1], 0.0f);
+                    reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+                } else if (EPI == EPI_BIAS_F32) {
+                    *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + cell * COUT + ch) =
+                        make_float2(v0 + bias[ch], v1 + bias[ch + 1]);
+                } else {
+                    const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask + cell * COUT + ch);
+                    v0 = __bfloat162float(mk.x) > 0.0f ? v0 : 0.0f;
+                    v1 = __bfloat162float(mk.y) > 0.0f ? v1 : 0.0f;
+                    reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+                }
             }
         }
     }
@@ -140,7 +149,7 @@ __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16
 
 template <int CIN, int COUT>
 constexpr size_t conv_smem_bytes() {
-    return (size_t)(3 * (CONV_CELLS + 2) + 9 * COUT) * SmemStride<CIN>::WORDS * 4;
+    return (size_t)((CONV_ROWS + 2) * (CONV_CELLS + 2) + 9 * COUT) * SmemStride<CIN>::WORDS * 4;
 }
 
 // Weight gradients of one layer, FP32 on the CUDA cores:

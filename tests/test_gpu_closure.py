@@ -73,6 +73,10 @@ def test_targets_match_restatement(gpu, target, projection):
     """With all parameters zero the network output is 0, so the loss of one pair is the
     mean square of the stored target over the crop's interior."""
     n, S, s_out = 128, 32, 2000.0
+    if target == "momentum" and projection == "cell":  # P would remove the whole target
+        with pytest.raises(Exception):
+            Closure(n, n, seed=5, s_out=s_out, inputs="eq", target=target, projection=projection)
+        return
     c = Closure(n, n, seed=5, s_out=s_out, inputs="eq", target=target, projection=projection)
     c.params = np.zeros(c.nparams, np.float32)
     c.reserve(2, S, 1)
