@@ -73,7 +73,8 @@ extern "C" {
 #define LBM_DTYPE_BF16 3 /* physics mode only: f_i - w_i in BF16, FP32 arithmetic */
 
 /* step kernel variants (physics mode) */
-#define LBM_KERNEL_AUTO 0   /* the fastest measured variant: currently LBM_KERNEL_CELL */
+#define LBM_KERNEL_AUTO 0   /* the fastest measured variant: LBM_KERNEL_CELL for FP32 / FP64,
+                               LBM_KERNEL_VEC2 for FP16 / BF16 (nx even) */
 #define LBM_KERNEL_CELL 1   /* one cell per thread */
 #define LBM_KERNEL_VEC4 2   /* four cells per thread, vector loads and stores (nx % 4 == 0) */
 #define LBM_KERNEL_BULK 3   /* four cells per thread fed by double-buffered bulk asynchronous

@@ -19,12 +19,13 @@ constexpr double MRT_S_E = 1.1, MRT_S_EPS = 1.0, MRT_S_Q = 1.2;
 // Boundary rules on the pulled populations d (Zou-He inlet, anchored outflow), moments,
 // Guo forcing with countdown, BGK.  o receives the post-collision deviations; rho, ux, uy
 // the macroscopic values of the cell.
-template <class R, int COLL = LBM_COLLISION_BGK>
+template <class R, int COLL = LBM_COLLISION_BGK, bool PLAIN = false>
 __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size_t c, uint16_t* __restrict__ flags,
                                              lbm_lattice_info* __restrict__ info, R omega, R (&o)[9], R& rho_out,
                                              R& ux_out, R& uy_out, const R U = R(1)) {
-    const bool outlet = (m == LBM_OUTLET);
-    if (m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
+    // PLAIN: the caller knows the cell is plain fluid (no inlet, outlet or forcing rule)
+    const bool outlet = !PLAIN && (m == LBM_OUTLET);
+    if (!PLAIN && m == LBM_INLET) {  // Zou-He velocity inlet, west face: unknowns 1, 5, 8
         const lbm_lattice_info in = info[c];
         const R ux = R(in.vx), uy = R(in.vy);
         const R S = d[0] + d[2] + d[4] + R(2) * (d[3] + d[6] + d[7]);
@@ -45,7 +46,7 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
     R jy = (d[4] - d[2]) + ((d[7] - d[5]) + (d[8] - d[6]));
     const R rho = U + drho;
     R Fx = R(0), Fy = R(0);
-    const bool forced = (m == LBM_EXTERNAL_FORCE);
+    const bool forced = !PLAIN && (m == LBM_EXTERNAL_FORCE);
     if (forced) {  // Guo forcing with the reference's block_iter countdown
         lbm_lattice_info in = info[c];
         if (in.block_iter > 0) {

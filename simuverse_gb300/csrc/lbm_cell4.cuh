@@ -139,7 +139,9 @@ struct VecN<ST, 4> : Vec4<ST> {};
 template <class ST>
 struct VecN<ST, 2> : Vec2<ST> {};
 
-template <class ST, bool MACRO, int CPT = 4>
+// IDX: the integer type of element offsets (uint32_t when 9 * pitch * ny < 2^32, which saves
+// the 64-bit address arithmetic of every plane access; size_t otherwise)
+template <class ST, bool MACRO, int CPT = 4, class IDX = size_t>
 __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                    typename ST::R omega, int x0, int y, int nx, int pitch, int ny,
@@ -147,9 +149,9 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
     using R = typename ST::R;
     using T = typename ST::T;
     const int lane = threadIdx.x & 31;
-    const size_t N = (size_t)pitch * ny;
+    const IDX N = (IDX)pitch * (IDX)ny;
     const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const size_t r0 = (size_t)y * pitch, rm = (size_t)ym * pitch, rp = (size_t)yp * pitch;
+    const IDX r0 = (IDX)y * (IDX)pitch, rm = (IDX)ym * (IDX)pitch, rp = (IDX)yp * (IDX)pitch;
     const int xl = x0 == 0 ? nx - 1 : x0 - 1;
     const int xr = x0 + CPT >= nx ? 0 : x0 + CPT;
     const bool own_left = lane == 0;
@@ -160,10 +162,10 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
     for (int k = 0; k < CPT; ++k) fl[k] = LBM_BOUNDARY;
     if (active) {
         if (CPT == 4) {
-            const uint2 q = *reinterpret_cast<const uint2*>(flags + r0 + x0);
+            const uint2 q = *reinterpret_cast<const uint2*>(flags + (r0 + (IDX)x0));
             fl[0] = q.x & 0xffffu; fl[1] = q.x >> 16; fl[CPT > 2 ? 2 : 0] = q.y & 0xffffu; fl[CPT > 3 ? 3 : 0] = q.y >> 16;
         } else {
-            const unsigned q = *reinterpret_cast<const unsigned*>(flags + r0 + x0);
+            const unsigned q = *reinterpret_cast<const unsigned*>(flags + (r0 + (IDX)x0));
             fl[0] = q & 0xffffu; fl[1] = q >> 16;
         }
     }
@@ -171,12 +173,12 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
     R d[9][CPT];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
-        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        const T* Aj = A + (size_t)j * N + row;
+        const IDX row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+        const T* Aj = A + ((IDX)j * N + row);
         R v[CPT];
 #pragma unroll
         for (int k = 0; k < CPT; ++k) v[k] = R(0);
-        if (active) VecN<ST, CPT>::ld(Aj + x0, v);
+        if (active) VecN<ST, CPT>::ld(Aj + (IDX)x0, v);
         if (EX(j) == 0) {
 #pragma unroll
             for (int k = 0; k < CPT; ++k) d[j][k] = v[k];
@@ -198,15 +200,37 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             }
         }
     }
+    // warp-uniform fast path: every cell of the warp is plain fluid (bulk, ghost or unknown
+    // material, no solid pull source) -- no boundary rule to test per cell
+    bool plain = true;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const unsigned mat = fl[k] & FL_MAT_MASK;
+        plain = plain && (mat == LBM_BULK || mat == LBM_GHOST || mat == 0u) && !(fl[k] & (0x1FFu << FL_DIR_SHIFT)) &&
+                x0 + k < nx;
+    }
+    const bool fast = __all_sync(0xffffffffu, !active || plain);
     if (!active) return;
 
     R mr[CPT], mu[CPT], mv[CPT];
+    if (fast) {
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            R dk[9], o[9];
+#pragma unroll
+            for (int j = 0; j < 9; ++j) dk[j] = d[j][k];
+            phys_collide<R, LBM_COLLISION_BGK, true>(dk, LBM_BULK, fl[k], (size_t)(r0 + (IDX)(x0 + k)), flags, info, omega, o, mr[k],
+                                                     mu[k], mv[k], R(ST::UNIT));
+#pragma unroll
+            for (int j = 0; j < 9; ++j) d[j][k] = o[j];
+        }
+    } else {
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
         const unsigned f = fl[k];
         const int m = (int)(f & FL_MAT_MASK);
         const int x = x0 + k;
-        const size_t c = r0 + x;
+        const IDX c = r0 + (IDX)x;
         R dk[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) dk[j] = d[j][k];
@@ -217,20 +241,20 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             continue;
         }
         if (m == LBM_OUTLET) {  // zero-gradient: e_x = -1 populations come from the own column
-            dk[3] = ST::ldu(A + 3 * N + r0 + x);
-            dk[6] = ST::ldu(A + 6 * N + rp + x);
-            dk[7] = ST::ldu(A + 7 * N + rm + x);
+            dk[3] = ST::ldu(A + (3 * N + r0 + (IDX)x));
+            dk[6] = ST::ldu(A + (6 * N + rp + (IDX)x));
+            dk[7] = ST::ldu(A + (7 * N + rm + (IDX)x));
         }
         if (f & (0xFFu << (FL_DIR_SHIFT + 1))) {  // some pull source is solid: bounce back
 #pragma unroll
             for (int j = 1; j < 9; ++j) {
                 if (f & (1u << (FL_DIR_SHIFT + j))) {
-                    R v = ST::ldu(A + c + (size_t)INV(j) * N);
+                    R v = ST::ldu(A + (c + (IDX)INV(j) * N));
                     if (f & FL_MOVING) {
                         int sx = x - EX(j);
                         if (m == LBM_OUTLET && EX(j) == -1) sx = x;
                         sx = sx < 0 ? nx - 1 : (sx >= nx ? 0 : sx);
-                        const size_t srow = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+                        const IDX srow = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
                         const lbm_lattice_info si = info[srow + sx];
                         const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
                         if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j) * R(ST::UNIT), uw));
@@ -240,18 +264,19 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             }
         }
         R o[9];
-        phys_collide<R>(dk, m, f, c, flags, info, omega, o, mr[k], mu[k], mv[k], R(ST::UNIT));
+        phys_collide<R>(dk, m, f, (size_t)c, flags, info, omega, o, mr[k], mu[k], mv[k], R(ST::UNIT));
 #pragma unroll
         for (int j = 0; j < 9; ++j) d[j][k] = o[j];
     }
+    }
 #pragma unroll
-    for (int j = 0; j < 9; ++j) VecN<ST, CPT>::st(B + (size_t)j * N + r0 + x0, d[j]);
+    for (int j = 0; j < 9; ++j) VecN<ST, CPT>::st(B + ((IDX)j * N + r0 + (IDX)x0), d[j]);
     if (MACRO) {
 #pragma unroll
         for (int k = 0; k < CPT; ++k) {
-            macro[r0 + x0 + k] = (float)mr[k];
-            macro[N + r0 + x0 + k] = (float)mu[k];
-            macro[2 * N + r0 + x0 + k] = (float)mv[k];
+            macro[r0 + (IDX)(x0 + k)] = (float)mr[k];
+            macro[N + r0 + (IDX)(x0 + k)] = (float)mu[k];
+            macro[2 * N + r0 + (IDX)(x0 + k)] = (float)mv[k];
         }
     }
 }

@@ -551,8 +551,9 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
             k_ref_step<false><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
         return cudaGetLastError();
     }
-    // auto = one cell per thread, the fastest variant measured on GB300 (86.8 % of the HBM
-    // copy bandwidth at 4096^2 against 70.9 % for VEC4 and 68.6 % for BULK)
+    // auto = the fastest variant measured on GB300: one cell per thread for FP32 and FP64
+    // (94.9 % of the HBM copy bandwidth at 4096^2 FP32, against 70.9 % for VEC4 and 68.6 % for
+    // BULK), two cells per thread for 16-bit storage (130 against 112 GLUPS at 8192^2 FP16)
     if (h->p.collision != LBM_COLLISION_BGK) {  // the vector kernels implement BGK only
         switch (h->p.dtype) {
             case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
@@ -564,6 +565,9 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     if (h->p.kernel == LBM_KERNEL_BULK) return launch_phys_step_bulk(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);
+    if (h->p.kernel == LBM_KERNEL_AUTO && (h->p.dtype == LBM_DTYPE_F16 || h->p.dtype == LBM_DTYPE_BF16) &&
+        h->nx % 2 == 0)
+        return launch_phys_step_vec2(h, write_macro, s);
     switch (h->p.dtype) {
         case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);
         case LBM_DTYPE_F64: return write_macro ? phys_step_t<StoreF64, true>(h, s) : phys_step_t<StoreF64, false>(h, s);

@@ -12,19 +12,22 @@ namespace lbm {
 
 constexpr int VEC_TPB = 128;  // 512 cells of a row per block
 
-template <class ST, bool MACRO>
+template <class ST, bool MACRO, class IDX>
 __global__ void __launch_bounds__(VEC_TPB) k_phys_step_v4(const typename ST::T* __restrict__ A,
                                                           typename ST::T* __restrict__ B, uint16_t* __restrict__ flags,
                                                           lbm_lattice_info* __restrict__ info, typename ST::R omega,
                                                           int nx, int ny, float* __restrict__ macro) {
     const int x0 = (blockIdx.x * VEC_TPB + threadIdx.x) * 4;
-    phys_cells4_update<ST, MACRO>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
+    phys_cells4_update<ST, MACRO, 4, IDX>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
 }
+
+// 32-bit element offsets are exact when every offset (9 planes, 3 macro planes) stays below 2^32
+static inline bool idx32_ok(const lbm_handle* h) { return (size_t)9 * h->N < ((size_t)1 << 32); }
 
 // two cells per thread: one 32-bit access per plane for FP16 / BF16 (threads that walk
 // several rows, amortising the column set-up, measured slower: register spills at 48
 // registers, or lower occupancy at 64)
-template <class ST, bool MACRO>
+template <class ST, bool MACRO, class IDX>
 __global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_v2(const typename ST::T* __restrict__ A,
                                                               typename ST::T* __restrict__ B,
                                                               uint16_t* __restrict__ flags,
@@ -32,7 +35,7 @@ __global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_v2(const typename ST:
                                                               typename ST::R omega, int nx, int ny,
                                                               float* __restrict__ macro) {
     const int x0 = (blockIdx.x * VEC_TPB + threadIdx.x) * 2;
-    phys_cells4_update<ST, MACRO, 2>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
+    phys_cells4_update<ST, MACRO, 2, IDX>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
 }
 
 template <class ST, bool MACRO>
@@ -41,8 +44,12 @@ static cudaError_t phys_step_v2_t(lbm_handle* h, cudaStream_t s) {
     using R = typename ST::R;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     const dim3 grid((unsigned)((h->nx / 2 + VEC_TPB - 1) / VEC_TPB), (unsigned)h->ny);
-    k_phys_step_v2<ST, MACRO><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, omega, h->nx, h->ny, h->d_macro);
+    if (idx32_ok(h))
+        k_phys_step_v2<ST, MACRO, uint32_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                                    h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
+    else
+        k_phys_step_v2<ST, MACRO, size_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                                  h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
 }
 
@@ -61,8 +68,12 @@ static cudaError_t phys_step_v4_t(lbm_handle* h, cudaStream_t s) {
     using R = typename ST::R;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     const dim3 grid((unsigned)((h->nx / 4 + VEC_TPB - 1) / VEC_TPB), (unsigned)h->ny);
-    k_phys_step_v4<ST, MACRO><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags,
-                                                        h->d_info, omega, h->nx, h->ny, h->d_macro);
+    if (idx32_ok(h))
+        k_phys_step_v4<ST, MACRO, uint32_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                                    h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
+    else
+        k_phys_step_v4<ST, MACRO, size_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                                  h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
 }
 
