@@ -54,6 +54,23 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(pg, x: float, device) -> float:
+    """The largest x over the ranks of pg (x itself without a process group)."""
+    if pg is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_glups(world: int, cells: int, steps: int, seconds_max: float) -> float:
+    """Whole-job GLUPS of `world` independent replicas of `cells` cells, each stepped
+    `steps` times, timed by the slowest replica (weak scaling: no data is exchanged)."""
+    return world * cells * steps / seconds_max / 1e9
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
 
@@ -219,12 +236,8 @@ def run_gpu(args):
     ms = ev0.elapsed_time(ev1)
     gpu_launches = sim.kernel_launches - launches0
     clk = clocks.stop()
-    ms_max = ms
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * cells * args.steps / (ms_max * 1e-3) / 1e9
+    ms_max = max_over_ranks(pg, ms, "cuda")
+    value = replica_glups(world, cells, args.steps, ms_max * 1e-3)
     per_launch_s = ms * 1e-3 / args.steps
     bytes_per_cell = 18 * BYTES_PER_VALUE[args.dtype]
     achieved = bytes_per_cell * cells / per_launch_s / 1e9
@@ -259,11 +272,7 @@ def run_gpu(args):
     t_e2e = time.perf_counter() - t0
     s2.close()
     assert np.isfinite(rho).all()
-    e2e_glups = cells * args.steps / t_e2e / 1e9
-    if pg:
-        t = torch.tensor([t_e2e], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_glups = world * cells * args.steps / float(t.item()) / 1e9
+    e2e_glups = replica_glups(world, cells, args.steps, max_over_ranks(pg, t_e2e, "cuda"))
     h2d = cells * 16  # info records uploaded at creation
     d2h = cells * 12  # rho, ux, uy read back
 
