@@ -219,8 +219,11 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
             R dk[9], o[9];
 #pragma unroll
             for (int j = 0; j < 9; ++j) dk[j] = d[j][k];
-            phys_collide<R, LBM_COLLISION_BGK, true>(dk, LBM_BULK, fl[k], (size_t)(r0 + (IDX)(x0 + k)), flags, info, omega, o, mr[k],
-                                                     mu[k], mv[k], R(ST::UNIT));
+            if constexpr (ST::dtype == LBM_DTYPE_F16 || ST::dtype == LBM_DTYPE_BF16)
+                bgk_plain_fast(dk, omega, R(ST::UNIT), o, mr[k], mu[k], mv[k]);
+            else
+                phys_collide<R, LBM_COLLISION_BGK, true>(dk, LBM_BULK, fl[k], (size_t)(r0 + (IDX)(x0 + k)), flags, info,
+                                                         omega, o, mr[k], mu[k], mv[k], R(ST::UNIT));
 #pragma unroll
             for (int j = 0; j < 9; ++j) d[j][k] = o[j];
         }
