@@ -73,14 +73,19 @@ extern "C" {
 #define LBM_DTYPE_BF16 3 /* physics mode only: f_i - w_i in BF16, FP32 arithmetic */
 
 /* step kernel variants (physics mode) */
-#define LBM_KERNEL_AUTO 0   /* the fastest measured variant: LBM_KERNEL_CELL for FP32 / FP64,
-                               LBM_KERNEL_VEC2 for FP16 / BF16 (nx even) */
+#define LBM_KERNEL_AUTO 0   /* the fastest measured variant: LBM_KERNEL_CELL for FP32 / FP64;
+                               for FP16 / BF16 LBM_KERNEL_TILED where it applies, else
+                               LBM_KERNEL_VEC2 (nx even) */
 #define LBM_KERNEL_CELL 1   /* one cell per thread */
 #define LBM_KERNEL_VEC4 2   /* four cells per thread, vector loads and stores (nx % 4 == 0) */
 #define LBM_KERNEL_BULK 3   /* four cells per thread fed by double-buffered bulk asynchronous
                                copies into shared memory, persistent blocks (nx % 8 == 0) */
 #define LBM_KERNEL_VEC2 4   /* two cells per thread, one 32-bit access per plane for 16-bit
                                storage (nx % 2 == 0) */
+#define LBM_KERNEL_TILED 5  /* two cells per thread over a tiled layout of 16-bit populations
+                               (the nine planes of 64 cells stored together; FP16 / BF16, BGK,
+                               nx % 64 == 0); read-back and checkpoints are layout-independent
+                               except that a checkpoint loads only into the same layout */
 
 /* physics-mode collision */
 #define LBM_COLLISION_BGK 0          /* single relaxation time */

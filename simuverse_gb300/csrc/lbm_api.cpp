@@ -229,7 +229,9 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "scene %d exists in physics mode only", p.scene);
     if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
-    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_VEC2) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_TILED) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if (p.kernel == LBM_KERNEL_TILED && !lbm::tiled_layout_eligible(p))
+        return fail(LBM_ERR_ARG, "the tiled kernel needs physics mode, FP16 or BF16 storage, BGK and nx %% 64 == 0");
     if (p.collision < LBM_COLLISION_BGK || p.collision > LBM_COLLISION_KBC)
         return fail(LBM_ERR_ARG, "unknown collision %d", p.collision);
     if (p.collision != LBM_COLLISION_BGK && p.mode != LBM_MODE_PHYSICS)
@@ -350,6 +352,7 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
     h->ny = p.ny;
     h->N = (size_t)p.nx * p.ny;
     h->fluid_ty = (p.scene == LBM_SCENE_CAVITY) ? 1 : 0;
+    h->tiled = (p.kernel == LBM_KERNEL_TILED || p.kernel == LBM_KERNEL_AUTO) && lbm::tiled_layout_eligible(p);
     h->tau = p.tau;
     h->omega = 1.0f / p.tau;
     h->omega_d = 1.0 / (double)p.tau;
@@ -827,6 +830,7 @@ struct ckpt_header {
     int32_t nx, ny, mode, dtype, scene, fluid_ty, cur;
     float tau, pre_x, pre_y;
     int32_t stepped;
+    int32_t layout;  // 1: tiled 16-bit populations (zero in checkpoints written before it existed)
     uint64_t steps;
 };
 
@@ -850,6 +854,7 @@ int lbm_save(lbm_handle* h, const char* path) {
     hd.nx = h->nx; hd.ny = h->ny; hd.mode = h->p.mode; hd.dtype = h->p.dtype; hd.scene = h->p.scene;
     hd.fluid_ty = h->fluid_ty; hd.cur = h->cur; hd.tau = h->tau; hd.pre_x = h->pre_x; hd.pre_y = h->pre_y;
     hd.stepped = h->stepped_since_init ? 1 : 0;
+    hd.layout = h->tiled ? 1 : 0;
     hd.steps = h->steps;
     FILE* f = std::fopen(path, "wb");
     if (!f) return fail(LBM_ERR_IO, "cannot open %s for writing", path);
@@ -877,6 +882,10 @@ int lbm_load(lbm_handle* h, const char* path) {
     if (hd.nx != h->nx || hd.ny != h->ny || hd.mode != h->p.mode || hd.dtype != h->p.dtype) {
         std::fclose(f);
         return fail(LBM_ERR_ARG, "checkpoint %dx%d mode %d dtype %d does not match the handle", hd.nx, hd.ny, hd.mode, hd.dtype);
+    }
+    if ((hd.layout != 0) != h->tiled) {
+        std::fclose(f);
+        return fail(LBM_ERR_ARG, "checkpoint population layout (%s) does not match the handle's", hd.layout ? "tiled" : "SoA");
     }
     const size_t pop_bytes = 9 * h->N * lbm::dtype_size(h->p.dtype);
     std::vector<char> state(2 * pop_bytes);

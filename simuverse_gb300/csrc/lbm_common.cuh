@@ -47,6 +47,15 @@ constexpr unsigned FL_MOVING = 1u << 13;
 
 __host__ __device__ constexpr bool is_solid(int m) { return m == LBM_BOUNDARY || m == LBM_OBSTACLE; }
 
+// Population layouts.  SoA (the reference's, d2q9_fn.wgsl:13-17): direction j of cell c at
+// j * N + c.  Tiled (16-bit storage with the two-cell kernel, nx % POP_TILE == 0): rows are
+// cut into tiles of POP_TILE cells and a tile keeps its nine planes together, direction j of
+// cell c at (c / POP_TILE) * 9 * POP_TILE + j * POP_TILE + c % POP_TILE.  Both use 9 N elements.
+constexpr int POP_TILE = 64;
+__host__ __device__ __forceinline__ size_t pop_index(bool tiled, size_t N, int j, size_t c) {
+    return tiled ? (c / POP_TILE) * (9 * POP_TILE) + (size_t)j * POP_TILE + (c % POP_TILE) : (size_t)j * N + c;
+}
+
 // round-to-nearest add and multiply that the compiler may not contract into an FMA
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }

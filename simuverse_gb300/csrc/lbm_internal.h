@@ -16,6 +16,7 @@ struct lbm_handle {
     int nx = 0, ny = 0;
     size_t N = 0;
     int fluid_ty = 0;  // d2q9_node.rs:53-57: 1 for the cavity, else 0
+    bool tiled = false;  // populations in the tiled layout (pop_index), 16-bit storage only
     float tau = 0.6f, omega = 1.0f / 0.6f;
     double omega_d = 1.0 / (double)0.6f;  // 1 / tau in FP64, for FP64 storage
     void* buf[2] = {nullptr, nullptr};  // ping-pong population buffers (9*N each)
@@ -62,6 +63,9 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s);
 bool vec_step_supported(const lbm_handle* h);
 cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s);
 cudaError_t launch_phys_step_vec2(lbm_handle* h, bool write_macro, cudaStream_t s);
+cudaError_t launch_phys_step_tiled(lbm_handle* h, bool write_macro, cudaStream_t s);
+// the tiled layout applies: physics mode, 16-bit storage, BGK, nx % POP_TILE == 0, 9 N < 2^32
+bool tiled_layout_eligible(const lbm_params& p);
 // bulk-copy fed physics step (lbm_step_bulk.cu)
 bool bulk_step_supported(const lbm_handle* h);
 cudaError_t launch_phys_step_bulk(lbm_handle* h, bool write_macro, cudaStream_t s);

@@ -113,7 +113,7 @@ template <class ST>
 __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                             const lbm_lattice_info* __restrict__ info, const float* __restrict__ rho_in,
                             const float* __restrict__ ux_in, const float* __restrict__ uy_in, int nx, int ny,
-                            float* __restrict__ macro) {
+                            float* __restrict__ macro, bool tiled) {
     using R = typename ST::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
@@ -122,7 +122,11 @@ __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __re
     const size_t c = (size_t)y * nx + x;
     if (is_solid(info[c].material)) {
 #pragma unroll
-        for (int i = 0; i < 9; ++i) { ST::st(A + c + i * N, R(0)); ST::st(B + c + i * N, R(0)); }
+        for (int i = 0; i < 9; ++i) {
+            const size_t k = pop_index(tiled, N, i, c);
+            ST::st(A + k, R(0));
+            ST::st(B + k, R(0));
+        }
         macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f;
         return;
     }
@@ -135,8 +139,9 @@ __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __re
     for (int i = 0; i < 9; ++i) {
         const R eu = R(EX(i)) * ux + R(EY(i)) * uy;
         const R d = PW<R>(i) * (drho + rho * (R(3) * eu + R(4.5) * (eu * eu) - usq));
-        ST::st(A + c + i * N, d);
-        ST::st(B + c + i * N, d);
+        const size_t k = pop_index(tiled, N, i, c);
+        ST::st(A + k, d);
+        ST::st(B + k, d);
     }
     macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy;
 }
@@ -265,7 +270,7 @@ __device__ __forceinline__ void block_reduce_sum(double (&v)[K], double* smem /*
 template <class ST, int MODE>
 __global__ void __launch_bounds__(RED_TPB) k_conservation(const typename ST::T* __restrict__ A,
                                                           const uint16_t* __restrict__ flags, size_t N,
-                                                          double* __restrict__ part) {
+                                                          double* __restrict__ part, bool tiled = false) {
     __shared__ double smem[3 * 32];
     double v[3] = {0.0, 0.0, 0.0};
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -275,7 +280,7 @@ __global__ void __launch_bounds__(RED_TPB) k_conservation(const typename ST::T* 
         if (MODE == LBM_MODE_PHYSICS) v[0] += 1.0;
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
-            const double f = (double)ST::to_r(A[c + (size_t)j * N]);
+            const double f = (double)ST::to_r(A[pop_index(tiled, N, j, c)]);
             v[0] += f;
             v[1] += (double)EX(j) * f;
             v[2] += (double)EY(j) * f;
@@ -391,25 +396,29 @@ __global__ void k_macro_rgba16f(const float* __restrict__ macro, const uint16_t*
     out[c] = o;
 }
 
+// dst / src: SoA host-order arrays (direction j of cell c at j * N + c) whatever the state's layout
 template <class ST, class D>
-__global__ void k_to_absolute(const typename ST::T* __restrict__ s, D* __restrict__ dst, size_t N, int mode) {
+__global__ void k_to_absolute(const typename ST::T* __restrict__ s, D* __restrict__ dst, size_t N, int mode,
+                              bool tiled) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 9 * N) return;
     const int j = (int)(i / N);
     using R = typename ST::R;
-    const R v = ST::to_r(s[i]);
+    const R v = ST::to_r(s[pop_index(tiled, N, j, i - (size_t)j * N)]);
     if (mode == LBM_MODE_REFERENCE) dst[i] = (D)v;
     else dst[i] = (D)PW<D>(j) + (D)v;
 }
 
 template <class ST, class D>
-__global__ void k_from_absolute(const D* __restrict__ src, typename ST::T* __restrict__ s, size_t N, int mode) {
+__global__ void k_from_absolute(const D* __restrict__ src, typename ST::T* __restrict__ s, size_t N, int mode,
+                                bool tiled) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 9 * N) return;
     const int j = (int)(i / N);
     using R = typename ST::R;
-    if (mode == LBM_MODE_REFERENCE) s[i] = ST::from_r((R)src[i]);
-    else s[i] = ST::from_r((R)(src[i] - PW<D>(j)));
+    const size_t k = pop_index(tiled, N, j, i - (size_t)j * N);
+    if (mode == LBM_MODE_REFERENCE) s[k] = ST::from_r((R)src[i]);
+    else s[k] = ST::from_r((R)(src[i] - PW<D>(j)));
 }
 
 // ------------------------------------------------------------------------------------
@@ -507,7 +516,7 @@ cudaError_t launch_ref_init(lbm_handle* h, cudaStream_t s) {
 template <class ST>
 static cudaError_t phys_init_t(lbm_handle* h, const float* r, const float* ux, const float* uy, cudaStream_t s) {
     k_phys_init<ST><<<cell_grid(h), TPB, 0, s>>>((typename ST::T*)h->buf[0], (typename ST::T*)h->buf[1], h->d_info, r, ux,
-                                                 uy, h->nx, h->ny, h->d_macro);
+                                                 uy, h->nx, h->ny, h->d_macro, h->tiled);
     return cudaGetLastError();
 }
 
@@ -562,6 +571,7 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
             default: return write_macro ? phys_step_t<StoreBF16, true>(h, s) : phys_step_t<StoreBF16, false>(h, s);
         }
     }
+    if (h->tiled) return launch_phys_step_tiled(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_BULK) return launch_phys_step_bulk(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);
@@ -580,9 +590,9 @@ template <class ST>
 static cudaError_t conservation_t(lbm_handle* h, double* out, cudaStream_t s) {
     const auto* A = (const typename ST::T*)h->buf[h->cur];
     if (h->p.mode == LBM_MODE_REFERENCE)
-        k_conservation<ST, LBM_MODE_REFERENCE><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, h->d_flags, h->N, h->d_part);
+        k_conservation<ST, LBM_MODE_REFERENCE><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, h->d_flags, h->N, h->d_part, h->tiled);
     else
-        k_conservation<ST, LBM_MODE_PHYSICS><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, h->d_flags, h->N, h->d_part);
+        k_conservation<ST, LBM_MODE_PHYSICS><<<RED_BLOCKS, RED_TPB, 0, s>>>(A, h->d_flags, h->N, h->d_part, h->tiled);
     k_final_sum<3><<<1, RED_TPB, 0, s>>>(h->d_part, RED_BLOCKS, out);
     return cudaGetLastError();
 }
@@ -632,9 +642,11 @@ template <class ST>
 static cudaError_t to_abs_t(lbm_handle* h, const void* state, void* dst, int dd, cudaStream_t s) {
     const unsigned blocks = (unsigned)((9 * h->N + 255) / 256);
     if (dd == LBM_DTYPE_F64)
-        k_to_absolute<ST, double><<<blocks, 256, 0, s>>>((const typename ST::T*)state, (double*)dst, h->N, h->p.mode);
+        k_to_absolute<ST, double><<<blocks, 256, 0, s>>>((const typename ST::T*)state, (double*)dst, h->N, h->p.mode,
+                                                         h->tiled);
     else
-        k_to_absolute<ST, float><<<blocks, 256, 0, s>>>((const typename ST::T*)state, (float*)dst, h->N, h->p.mode);
+        k_to_absolute<ST, float><<<blocks, 256, 0, s>>>((const typename ST::T*)state, (float*)dst, h->N, h->p.mode,
+                                                        h->tiled);
     return cudaGetLastError();
 }
 
@@ -651,9 +663,11 @@ template <class ST>
 static cudaError_t from_abs_t(lbm_handle* h, const void* src, int sd, void* state, cudaStream_t s) {
     const unsigned blocks = (unsigned)((9 * h->N + 255) / 256);
     if (sd == LBM_DTYPE_F64)
-        k_from_absolute<ST, double><<<blocks, 256, 0, s>>>((const double*)src, (typename ST::T*)state, h->N, h->p.mode);
+        k_from_absolute<ST, double><<<blocks, 256, 0, s>>>((const double*)src, (typename ST::T*)state, h->N, h->p.mode,
+                                                           h->tiled);
     else
-        k_from_absolute<ST, float><<<blocks, 256, 0, s>>>((const float*)src, (typename ST::T*)state, h->N, h->p.mode);
+        k_from_absolute<ST, float><<<blocks, 256, 0, s>>>((const float*)src, (typename ST::T*)state, h->N, h->p.mode,
+                                                          h->tiled);
     return cudaGetLastError();
 }
 

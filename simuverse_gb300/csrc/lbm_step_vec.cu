@@ -5,6 +5,7 @@
 // Algorithmic traffic per cell update: 9 loads + 9 stores of the stored type (72 B FP32,
 // 36 B FP16/BF16, 144 B FP64) plus the 2-byte flag word.
 #include "lbm_cell4.cuh"
+#include "lbm_cell_tiled.cuh"
 #include "lbm_common.cuh"
 #include "lbm_internal.h"
 
@@ -75,6 +76,41 @@ static cudaError_t phys_step_v4_t(lbm_handle* h, cudaStream_t s) {
         k_phys_step_v4<ST, MACRO, size_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
                                                                   h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
     return cudaGetLastError();
+}
+
+// tiled 16-bit layout: one warp per 64-cell tile, consecutive warps along a row
+template <class ST, bool MACRO>
+__global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_tiled(const typename ST::T* __restrict__ A,
+                                                                 typename ST::T* __restrict__ B,
+                                                                 uint16_t* __restrict__ flags,
+                                                                 lbm_lattice_info* __restrict__ info, float omega,
+                                                                 int nx, int ny, float* __restrict__ macro) {
+    const int warp = (int)((blockIdx.x * VEC_TPB + threadIdx.x) >> 5);
+    const int tpr = nx / POP_TILE;
+    if (warp >= tpr * ny) return;  // whole warps
+    const int y = warp / tpr;
+    phys_tile_update<ST, MACRO>(A, B, flags, info, omega, warp - y * tpr, y, nx, ny, macro);
+}
+
+bool tiled_layout_eligible(const lbm_params& p) {
+    return p.mode == LBM_MODE_PHYSICS && (p.dtype == LBM_DTYPE_F16 || p.dtype == LBM_DTYPE_BF16) &&
+           p.collision == LBM_COLLISION_BGK && p.nx % POP_TILE == 0 && (size_t)9 * p.nx * p.ny < ((size_t)1 << 32);
+}
+
+template <class ST, bool MACRO>
+static cudaError_t phys_step_tiled_t(lbm_handle* h, cudaStream_t s) {
+    using T = typename ST::T;
+    const size_t threads = (size_t)(h->nx / POP_TILE) * h->ny * 32;
+    const unsigned blocks = (unsigned)((threads + VEC_TPB - 1) / VEC_TPB);
+    k_phys_step_tiled<ST, MACRO><<<blocks, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                            h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phys_step_tiled(lbm_handle* h, bool write_macro, cudaStream_t s) {
+    if (h->p.dtype == LBM_DTYPE_F16)
+        return write_macro ? phys_step_tiled_t<StoreF16, true>(h, s) : phys_step_tiled_t<StoreF16, false>(h, s);
+    return write_macro ? phys_step_tiled_t<StoreBF16, true>(h, s) : phys_step_tiled_t<StoreBF16, false>(h, s);
 }
 
 bool vec_step_supported(const lbm_handle* h) { return h->p.mode == LBM_MODE_PHYSICS && (h->nx % 4) == 0; }
