@@ -318,7 +318,7 @@ def run_precision(args):
     base = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
                 seed=1234)
     for dtype in () if args.skip_glups else ("f32", "f16", "bf16"):
-        for kernel in ("cell", "vec2", "vec4", "bulk"):
+        for kernel in ("cell", "vec2", "vec4", "bulk") + (("tiled",) if dtype != "f32" else ()):
             sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel, **base)
             sim.set_stream(stream.cuda_stream)
             sim.step(args.warmup)
