@@ -547,7 +547,7 @@ def main():
     ap.add_argument("--ny", type=int, default=4096)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2", "tiled"])
     ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch", "closure", "view"])
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snapshots", type=int, default=125)

@@ -235,6 +235,38 @@ __global__ void k_curl(Field f, float* __restrict__ out) {
     out[(size_t)y * f.nx + x] = h16(add_rn(mul_rn(curl, 3.5f), 0.5f));
 }
 
+// the same for four consecutive cells x0..x0+3 per thread (nx % 4 == 0, so x0 + 3 < nx): one
+// 16-byte load per row and plane, the left / right neighbours of the row y by scalar loads
+__global__ void k_curl4(Field f, float* __restrict__ out) {
+    const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x), y = blockIdx.y;
+    if (x0 >= f.nx) return;
+    float4 r;
+    if (f.zero) {
+        const float c = h16(0.5f);  // curl 0 stored as 0 * 3.5 + 0.5
+        r = make_float4(c, c, c, c);
+    } else {
+        const int yt = y - 1 < 0 ? 0 : y - 1, yb = y + 1 > f.ny - 1 ? f.ny - 1 : y + 1;  // clamped rows
+        const float4 T = __ldg(reinterpret_cast<const float4*>(f.ux + (size_t)yt * f.nx + x0));
+        const float4 Bv = __ldg(reinterpret_cast<const float4*>(f.ux + (size_t)yb * f.nx + x0));
+        const float* uyr = f.uy + (size_t)y * f.nx;
+        const float4 M = __ldg(reinterpret_cast<const float4*>(uyr + x0));
+        const float l = __ldg(uyr + (x0 > 0 ? x0 - 1 : 0));
+        const float rr = __ldg(uyr + (x0 + 4 < f.nx ? x0 + 4 : f.nx - 1));
+        const float uy[6] = {h16(l), h16(M.x), h16(M.y), h16(M.z), h16(M.w), h16(rr)};
+        const float tx[4] = {h16(T.x), h16(T.y), h16(T.z), h16(T.w)};
+        const float bx[4] = {h16(Bv.x), h16(Bv.y), h16(Bv.z), h16(Bv.w)};
+        float o[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // left neighbour of x0 + k is uy[k] (clamped at x = 0 by the load above), right is uy[k + 2]
+            const float curl = sub_rn(add_rn(sub_rn(uy[k + 2], uy[k]), tx[k]), bx[k]);
+            o[k] = h16(add_rn(mul_rn(curl, 3.5f), 0.5f));
+        }
+        r = make_float4(o[0], o[1], o[2], o[3]);
+    }
+    *reinterpret_cast<float4*>(out + (size_t)y * f.nx + x0) = r;
+}
+
 // linear-filtered, clamp-to-edge sample of a texel field at texture coordinate (u, v)
 template <class F>
 __device__ __forceinline__ float3 sample_linear(F fetch, int nx, int ny, float u, float v) {
@@ -557,8 +589,13 @@ int lbm_particles_counters(const lbm_particles* ps, uint64_t* updates, uint64_t*
 int lbm_curl(lbm_handle* h, float* d_out) {
     if (!h || !d_out) return vfail(LBM_ERR_ARG, "null argument");
     V_CK(cudaSetDevice(h->device));
-    const dim3 grid((unsigned)((h->nx + 127) / 128), (unsigned)h->ny);
-    view::k_curl<<<grid, 128, 0, h->stream>>>(field_of(h), d_out);
+    if (h->nx % 4 == 0 && ((uintptr_t)d_out & 15) == 0) {
+        const dim3 grid((unsigned)((h->nx / 4 + 127) / 128), (unsigned)h->ny);
+        view::k_curl4<<<grid, 128, 0, h->stream>>>(field_of(h), d_out);
+    } else {
+        const dim3 grid((unsigned)((h->nx + 127) / 128), (unsigned)h->ny);
+        view::k_curl<<<grid, 128, 0, h->stream>>>(field_of(h), d_out);
+    }
     V_CK(cudaGetLastError());
     ++h->launches;
     return LBM_OK;

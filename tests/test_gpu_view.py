@@ -111,3 +111,12 @@ def test_colorize_matches_oracle(gpu, mode):
         assert got.shape == ref.shape
         assert np.max(np.abs(got - ref)) < 1e-5, np.max(np.abs(got - ref))
     sim.close()
+
+
+def test_curl_scalar_path_matches_oracle(gpu):
+    """nx % 4 != 0 takes the one-cell curl kernel."""
+    sim = FluidSimulator(98, 50, mode="physics", scene="cavity", tau=0.6, lid_speed=0.1)
+    sim.step(30)
+    _, ux, uy = sim.read_macro()
+    assert np.array_equal(curl(sim), oracle.curl(ux, uy))
+    sim.close()
