@@ -4,8 +4,9 @@
 //          -> conv3x3 32->32 + bias, ReLU -> x2 -> conv3x3 32->9 (stored as 16) + bias -> y.
 // Activations are BF16 in NHWC order ([image][row][column][channel]); accumulation is FP32.
 // The convolutions are implicit GEMMs on the tensor cores with mma.sync.m16n8k16 (BF16 in,
-// FP32 accumulate): a warp owns 16 consecutive cells of one row (GEMM rows) times all output
-// channels (GEMM columns); K runs over the 9 taps x input channels.  The block stages the 3
+// FP32 accumulate), fragments loaded with ldmatrix: a warp owns 16 consecutive cells of one
+// row (GEMM rows) times all output channels (GEMM columns); K runs over the 9 taps x input
+// channels.  The block stages the 3
 // input rows it needs (64 + 2 cells each) and all weights in shared memory with a padded
 // per-cell stride of (C/2 + 4) words, which makes every fragment load bank-conflict free.
 //
@@ -35,6 +36,15 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], unsigned a0, unsig
         "{%0,%1,%2,%3};"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// four 8x8 b16 matrices from shared memory, one row address per thread (threads 8i .. 8i+7
+// address the rows of matrix i); thread t receives row t/4, columns 2(t%4), 2(t%4)+1 of each
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const unsigned* row) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
 }
 
 __device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
@@ -97,50 +107,69 @@ __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16
     const int x0 = xs + warp * 16;
     if (x0 >= W) return;
     const int g = lane >> 2, c = lane & 3;
+    // ldmatrix row addresses: A (cells x channels): matrix m = lane / 8 holds cells 8 (m % 2) ..
+    // +7 and channels 8 (m / 2) .. +7 of the 16 x 16 k-chunk; B (out x in channels): matrices
+    // (n-tile 2p, k lo), (2p, k hi), (2p + 1, k lo), (2p + 1, k hi)
+    const int mi = lane >> 3, rr = lane & 7;
+    const int a_cell = warp * 16 + rr + 8 * (mi & 1), a_k = 4 * (mi >> 1);
+    const int b_row = rr + 8 * (mi >> 1), b_k = 4 * (mi & 1);
+    // two output rows at a time: the weight fragments serve both, and the two accumulator
+    // sets are independent chains of mma
 #pragma unroll 1
-    for (int r = 0; r < CONV_ROWS; ++r) {
-        const int y = y0 + r;
-        if (y >= H) break;
-        float acc[NT][4];
+    for (int r = 0; r < CONV_ROWS; r += 2) {
+        if (y0 + r >= H) break;
+        float acc[2][NT][4];
 #pragma unroll
-        for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
+        for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int n = 0; n < NT; ++n) acc[q][n][0] = acc[q][n][1] = acc[q][n][2] = acc[q][n][3] = 0.0f;
 #pragma unroll
         for (int tap = 0; tap < 9; ++tap) {
             const int dy = tap / 3, dx = tap % 3;  // staged row / column offsets (0..2)
-            const unsigned* ra = sin + ((r + dy) * ROWC + warp * 16 + g + dx) * CS;
-            const unsigned* rb = ra + 8 * CS;
+            const unsigned* ra = sin + ((r + dy) * ROWC + a_cell + dx) * CS + a_k;
+            const unsigned* rw = sw + (tap * COUT + b_row) * CS + b_k;
 #pragma unroll
             for (int kc = 0; kc < CIN / 16; ++kc) {
-                const unsigned a0 = ra[kc * 8 + c], a1 = rb[kc * 8 + c];
-                const unsigned a2 = ra[kc * 8 + c + 4], a3 = rb[kc * 8 + c + 4];
+                unsigned a0[4], a1[4];
+                ldsm_x4(a0, ra + kc * 8);
+                ldsm_x4(a1, ra + ROWC * CS + kc * 8);  // the next row (staged rows r + 1 + dy)
 #pragma unroll
-                for (int n = 0; n < NT; ++n) {
-                    const unsigned* wb = sw + (tap * COUT + n * 8 + g) * CS + kc * 8 + c;
-                    mma_bf16_16816(acc[n], a0, a1, a2, a3, wb[0], wb[4]);
+                for (int p = 0; p < NT / 2; ++p) {
+                    unsigned b[4];
+                    ldsm_x4(b, rw + 16 * p * CS + kc * 8);
+                    mma_bf16_16816(acc[0][2 * p], a0[0], a0[1], a0[2], a0[3], b[0], b[1]);
+                    mma_bf16_16816(acc[0][2 * p + 1], a0[0], a0[1], a0[2], a0[3], b[2], b[3]);
+                    mma_bf16_16816(acc[1][2 * p], a1[0], a1[1], a1[2], a1[3], b[0], b[1]);
+                    mma_bf16_16816(acc[1][2 * p + 1], a1[0], a1[1], a1[2], a1[3], b[2], b[3]);
                 }
             }
         }
         // epilogue: thread holds rows g, g+8 (cells x0+g, x0+g+8) and columns n*8 + 2c, +1
-        const size_t cell0 = img_off + (size_t)y * W + x0 + g;
 #pragma unroll
-        for (int n = 0; n < NT; ++n) {
-            const int ch = n * 8 + 2 * c;
+        for (int q = 0; q < 2; ++q) {
+            const int y = y0 + r + q;
+            if (y >= H) break;
+            const size_t cell0 = img_off + (size_t)y * W + x0 + g;
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const size_t cell = cell0 + 8 * h;
-                float v0 = acc[n][2 * h], v1 = acc[n][2 * h + 1];
-                if (EPI == EPI_BIAS_RELU) {
-                    v0 = fmaxf(v0 + bias[ch], 0.0f);
-                    v1 = fmaxf(v1 + bias[ch + 1], 0.0f);
-                    reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
-                } else if (EPI == EPI_BIAS_F32) {
-                    *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + cell * COUT + ch) =
-                        make_float2(v0 + bias[ch], v1 + bias[ch + 1]);
-                } else {
-                    const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask + cell * COUT + ch);
-                    v0 = __bfloat162float(mk.x) > 0.0f ? v0 : 0.0f;
-                    v1 = __bfloat162float(mk.y) > 0.0f ? v1 : 0.0f;
-                    reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+            for (int n = 0; n < NT; ++n) {
+                const int ch = n * 8 + 2 * c;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const size_t cell = cell0 + 8 * h;
+                    float v0 = acc[q][n][2 * h], v1 = acc[q][n][2 * h + 1];
+                    if (EPI == EPI_BIAS_RELU) {
+                        v0 = fmaxf(v0 + bias[ch], 0.0f);
+                        v1 = fmaxf(v1 + bias[ch + 1], 0.0f);
+                        reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+                    } else if (EPI == EPI_BIAS_F32) {
+                        *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + cell * COUT + ch) =
+                            make_float2(v0 + bias[ch], v1 + bias[ch + 1]);
+                    } else {
+                        const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask + cell * COUT + ch);
+                        v0 = __bfloat162float(mk.x) > 0.0f ? v0 : 0.0f;
+                        v1 = __bfloat162float(mk.y) > 0.0f ? v1 : 0.0f;
+                        reinterpret_cast<unsigned*>(out)[(cell * COUT + ch) / 2] = pack_bf16x2(v0, v1);
+                    }
                 }
             }
         }
