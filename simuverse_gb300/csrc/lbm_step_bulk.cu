@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(BULK_TPB) k_phys_step_bulk(const typename ST::
         const int st = it % BULK_STAGES;
         const unsigned parity = (unsigned)(it / BULK_STAGES) & 1u;
         const TileGeom g = tile_geom(t, tiles_per_row, nx);
-        // thread 0 waits with a time limit and the block follows its verdict, so the block
+        // thread 0 waits with a time limit and the block follows its outcome, so the block
         // leaves together (no thread is left behind at a __syncthreads)
         if (tid == 0) s_ok = mbar_wait_bounded(&bars[st], parity, BULK_WAIT_NS) ? 1 : 0;
         __syncthreads();
