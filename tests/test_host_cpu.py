@@ -13,7 +13,8 @@ from conftest import ROOT
 
 
 def _declared(header):
-    text = open(os.path.join(ROOT, "include", header)).read()
+    with open(os.path.join(ROOT, "include", header)) as f:
+        text = f.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(lbm_[a-z0-9_]+)\s*\(", text)))
 
