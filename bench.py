@@ -261,6 +261,20 @@ def run_gpu(args):
     sim.close()
     torch.cuda.synchronize()
 
+    # ---- the reference's own rules (reference mode, its Poiseuille scene) at the same size
+    glups_ref_mode = None
+    if args.dtype == "f32":
+        sim_r = FluidSimulator(args.nx, args.ny, mode="reference", scene="poiseuille", tau=0.56)
+        sim_r.set_stream(stream.cuda_stream)
+        sim_r.step(args.warmup)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim_r.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        glups_ref_mode = cells * args.steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        sim_r.close()
+
     # ---- end to end through the public API, host buffers
     if pg:
         pg.barrier()
@@ -288,6 +302,7 @@ def run_gpu(args):
                          "traffic_source": (tr or {}).get("source"),
                          "algorithmic_bytes_per_launch": bytes_per_cell * cells},
             "macro_every_step_glups": glups_macro,
+            "reference_mode_glups": glups_ref_mode,
             "e2e": {"value": e2e_glups, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps,
                     "what": "create (host mask build + upload) + K steps + macro read-back, wall clock"},

@@ -107,3 +107,16 @@ def test_oracle_particle_update_matches_numpy_restatement():
         assert np.array_equal(a, b), it
         assert np.array_equal(ca, cb), it
     assert np.count_nonzero(ca[..., 0]) > 0
+
+
+def test_particle_host_functions_reject_bad_input(native):
+    from simuverse_gb300.view import particle_params
+
+    a, b = ctypes.c_int32(), ctypes.c_int32()
+    for cw, ch, count in ((0, 10, 10), (10, 0, 10), (10, 10, 0), (-5, 10, 10)):
+        assert native.lbm_particles_grid(cw, ch, count, ctypes.byref(a), ctypes.byref(b)) < 0
+    p = particle_params(40, 30, count=1)
+    out = np.empty((4, 6), np.float32)
+    # a 1 x 1 grid has no spacing (the reference would divide by zero): refused
+    assert native.lbm_particles_init_state(ctypes.byref(p), 1, 1, out.ctypes.data_as(ctypes.c_void_p)) < 0
+    assert native.lbm_particles_init_state(None, 2, 2, out.ctypes.data_as(ctypes.c_void_p)) < 0
