@@ -267,40 +267,33 @@ __global__ void k_curl4(Field f, float* __restrict__ out) {
     *reinterpret_cast<float4*>(out + (size_t)y * f.nx + x0) = r;
 }
 
-// linear-filtered, clamp-to-edge sample of a texel field at texture coordinate (u, v)
-template <class F>
-__device__ __forceinline__ float3 sample_linear(F fetch, int nx, int ny, float u, float v) {
-    const float tx = sub_rn(mul_rn(u, (float)nx), 0.5f), ty = sub_rn(mul_rn(v, (float)ny), 0.5f);
-    const float fx0 = floorf(tx), fy0 = floorf(ty);
-    const float ax = sub_rn(tx, fx0), ay = sub_rn(ty, fy0);
-    const int x0 = (int)fx0, y0 = (int)fy0;
-    const float3 a = fetch(x0, y0), b = fetch(x0 + 1, y0), c = fetch(x0, y0 + 1), d = fetch(x0 + 1, y0 + 1);
-    const float bx = sub_rn(1.0f, ax), by = sub_rn(1.0f, ay);
-    float3 r;
-    r.x = add_rn(mul_rn(add_rn(mul_rn(a.x, bx), mul_rn(b.x, ax)), by), mul_rn(add_rn(mul_rn(c.x, bx), mul_rn(d.x, ax)), ay));
-    r.y = add_rn(mul_rn(add_rn(mul_rn(a.y, bx), mul_rn(b.y, ax)), by), mul_rn(add_rn(mul_rn(c.y, bx), mul_rn(d.y, ax)), ay));
-    r.z = add_rn(mul_rn(add_rn(mul_rn(a.z, bx), mul_rn(b.z, ax)), by), mul_rn(add_rn(mul_rn(c.z, bx), mul_rn(d.z, ax)), ay));
-    return r;
-}
-
 // one canvas pixel (px, py) of the field colour map: uv at the pixel centre, as the
-// full-screen triangle of bufferless.vs.wgsl interpolates it
+// full-screen triangle of bufferless.vs.wgsl interpolates it; every plane is sampled with
+// linear filtering and clamp-to-edge addressing, with exact FP32 weights
 __global__ void k_colorize(Field f, const float* __restrict__ curl, int cw, int ch, int mode, float4* __restrict__ rgba) {
     const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y;
     if (px >= cw) return;
     const float u = __fdiv_rn(add_rn((float)px, 0.5f), (float)cw), v = __fdiv_rn(add_rn((float)py, 0.5f), (float)ch);
-    const float3 m = sample_linear([&](int i, int j) { return texel(f, i, j); }, f.nx, f.ny, u, v);
+    // the four texels around (u, v), clamped to the edge, shared by every sampled plane
+    const float tx = sub_rn(mul_rn(u, (float)f.nx), 0.5f), ty = sub_rn(mul_rn(v, (float)f.ny), 0.5f);
+    const float fx0 = floorf(tx), fy0 = floorf(ty);
+    const float ax = sub_rn(tx, fx0), ay = sub_rn(ty, fy0), bx = sub_rn(1.0f, ax), by = sub_rn(1.0f, ay);
+    const int x0 = (int)fx0, y0 = (int)fy0;
+    const int xa = x0 < 0 ? 0 : (x0 > f.nx - 1 ? f.nx - 1 : x0), xb = x0 + 1 < 0 ? 0 : (x0 + 1 > f.nx - 1 ? f.nx - 1 : x0 + 1);
+    const int ya = y0 < 0 ? 0 : (y0 > f.ny - 1 ? f.ny - 1 : y0), yb = y0 + 1 < 0 ? 0 : (y0 + 1 > f.ny - 1 ? f.ny - 1 : y0 + 1);
+    const size_t i00 = (size_t)ya * f.nx + xa, i10 = (size_t)ya * f.nx + xb;
+    const size_t i01 = (size_t)yb * f.nx + xa, i11 = (size_t)yb * f.nx + xb;
+    auto lerp = [&](float a, float b, float c, float d) {
+        return add_rn(mul_rn(add_rn(mul_rn(a, bx), mul_rn(b, ax)), by), mul_rn(add_rn(mul_rn(c, bx), mul_rn(d, ax)), ay));
+    };
+    auto plane = [&](const float* p) {
+        return lerp(h16(__ldg(p + i00)), h16(__ldg(p + i10)), h16(__ldg(p + i01)), h16(__ldg(p + i11)));
+    };
+    float3 m = make_float3(0.0f, 0.0f, 0.0f);  // no step since initialisation: a zero field
+    if (!f.zero) m = make_float3(plane(f.ux), plane(f.uy), plane(f.rho));
     float4 out;
     if (mode == LBM_COLOR_CURL) {
-        const float cv = sample_linear(
-                             [&](int i, int j) {
-                                 i = i < 0 ? 0 : (i > f.nx - 1 ? f.nx - 1 : i);
-                                 j = j < 0 ? 0 : (j > f.ny - 1 ? f.ny - 1 : j);
-                                 const float c = curl ? __ldg(curl + (size_t)j * f.nx + i) : 0.0f;
-                                 return make_float3(c, 0.0f, 0.0f);
-                             },
-                             f.nx, f.ny, u, v)
-                             .x;
+        const float cv = curl ? lerp(__ldg(curl + i00), __ldg(curl + i10), __ldg(curl + i01), __ldg(curl + i11)) : 0.0f;
         const float speed = add_rn(fabsf(m.x), fabsf(m.y));
         const float3 col = hsv2rgb(cv, add_rn(0.6f, mul_rn(speed, 1.4f)), add_rn(0.6f, mul_rn(m.z, 0.33f)));
         out = make_float4(col.x, col.y, col.z, m.z);
