@@ -149,40 +149,49 @@ __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __re
 // ------------------------------------------------------------------------------------
 // reference-mode step: collide_stream.wgsl:25-88 + boundary.wgsl:3-35, one pass
 // ------------------------------------------------------------------------------------
-template <bool MACRO>
+template <bool MACRO, class IDX>
 __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, float* __restrict__ B,
                                                   uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                   float omega, int nx, int ny, float* __restrict__ macro) {
     const int x = blockIdx.x * TPB + threadIdx.x;
     const int y = blockIdx.y;
     if (x >= nx) return;
-    const size_t N = (size_t)nx * ny;
-    const size_t c = (size_t)y * nx + x;
+    const IDX N = (IDX)nx * (IDX)ny;
+    const IDX c = (IDX)y * (IDX)nx + (IDX)x;
     const unsigned fl = flags[c];
     const int m = (int)(fl & FL_MAT_MASK);
     if (is_solid(m)) {  // collide_stream.wgsl:34-38
         if (MACRO) { macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f; }
 #pragma unroll
         for (int k = 0; k < 9; ++k)
-            if (fl & (1u << (FL_DIR_SHIFT + k))) B[c + k * N] = 0.0f;
+            if (fl & (1u << (FL_DIR_SHIFT + k))) B[c + (IDX)k * N] = 0.0f;
         return;
     }
+    // warp-uniform: no cell of the (active part of the) warp pushes into a wall slot or forces
+    const bool plain = !(fl & (0x1FFu << FL_DIR_SHIFT)) && m != LBM_INLET && m != LBM_EXTERNAL_FORCE;
+    const bool fast = __all_sync(__activemask(), plain);
     const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
     const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const size_t r0 = (size_t)y * nx, rm = (size_t)ym * nx, rp = (size_t)yp * nx;
+    const IDX r0 = (IDX)y * (IDX)nx, rm = (IDX)ym * (IDX)nx, rp = (IDX)yp * (IDX)nx;
     float f[9];
 #pragma unroll
     for (int j = 0; j < 9; ++j) {  // source uv - e(j), wrapped
         const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? xp : x);
-        const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        f[j] = __ldg(A + row + sx + (size_t)j * N);
+        const IDX row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+        f[j] = __ldg(A + (row + (IDX)sx + (IDX)j * N));
     }
+    // collide_stream.wgsl:40-48.  The terms e * f with e = 0 add a zero and those with e = +-1
+    // add or subtract f exactly, so they are written as such (populations are finite and
+    // clamped to [0, max], so the values are those of the literal expressions; only the sign of
+    // an exact zero may differ)
     float rho = 0.0f, vx = 0.0f, vy = 0.0f;
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
         rho = __fadd_rn(rho, f[j]);
-        vx = __fadd_rn(vx, __fmul_rn((float)EX(j), f[j]));
-        vy = __fadd_rn(vy, __fmul_rn((float)EY(j), f[j]));
+        if (EX(j) == 1) vx = __fadd_rn(vx, f[j]);
+        if (EX(j) == -1) vx = __fsub_rn(vx, f[j]);
+        if (EY(j) == 1) vy = __fadd_rn(vy, f[j]);
+        if (EY(j) == -1) vy = __fsub_rn(vy, f[j]);
     }
     rho = fminf(fmaxf(rho, 0.8f), 1.2f);
     vx = __fdiv_rn(vx, rho);
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
     float F[9];
 #pragma unroll
     for (int j = 0; j < 9; ++j) F[j] = 0.0f;
-    if (m == LBM_INLET || m == LBM_EXTERNAL_FORCE) {  // collide_stream.wgsl:55-71
+    if (!fast && (m == LBM_INLET || m == LBM_EXTERNAL_FORCE)) {  // collide_stream.wgsl:55-71
         lbm_lattice_info in = info[c];
         if (in.block_iter > 0) {
             in.block_iter = in.block_iter - 1;
@@ -212,18 +221,22 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
     const float usqr = __fmul_rn(1.5f, __fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)));
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
-        const float eu = __fadd_rn(__fmul_rn((float)EX(j), vx), __fmul_rn((float)EY(j), vy));
+        // e . u with e_x, e_y in {-1, 0, 1}: the same value as the literal products and sum
+        const float ex = EX(j) == 1 ? vx : (EX(j) == -1 ? -vx : 0.0f);
+        const float ey = EY(j) == 1 ? vy : (EY(j) == -1 ? -vy : 0.0f);
+        const float eu = (EX(j) == 0) ? ey : ((EY(j) == 0) ? ex : __fadd_rn(ex, ey));
         const float feq = __fmul_rn(__fmul_rn(rho, REF_W(j)),
                                     __fsub_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(3.0f, eu)), __fmul_rn(4.5f, __fmul_rn(eu, eu))),
                                               usqr));
-        float t = __fadd_rn(__fsub_rn(f[j], __fmul_rn(omega, __fsub_rn(f[j], feq))), F[j]);
+        float t = __fsub_rn(f[j], __fmul_rn(omega, __fsub_rn(f[j], feq)));
+        if (!fast) t = __fadd_rn(t, F[j]);  // + 0 when no force acts (the value is unchanged)
         if (t > REF_MAX(j)) t = REF_MAX(j);
         else if (t < 0.0f) t = 0.0f;
-        if (fl & (1u << (FL_DIR_SHIFT + j))) {
-            B[c + (size_t)EY(j) * nx + EX(j) + (size_t)INV(j) * N] = t;
-            B[c + (size_t)j * N] = 0.0f;
+        if (!fast && (fl & (1u << (FL_DIR_SHIFT + j)))) {
+            B[c + (IDX)(EY(j) * nx + EX(j)) + (IDX)INV(j) * N] = t;
+            B[c + (IDX)j * N] = 0.0f;
         } else {
-            B[c + (size_t)j * N] = t;
+            B[c + (IDX)j * N] = t;
         }
     }
 }
@@ -554,10 +567,19 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     if (h->p.mode == LBM_MODE_REFERENCE) {
         const float* A = (const float*)h->buf[h->cur];
         float* B = (float*)h->buf[h->cur ^ 1];
-        if (write_macro)
-            k_ref_step<true><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+        const bool idx32 = (size_t)9 * h->N < ((size_t)1 << 32);
+        if (write_macro && idx32)
+            k_ref_step<true, uint32_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
+                                                                    h->d_macro);
+        else if (write_macro)
+            k_ref_step<true, size_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
+                                                                  h->d_macro);
+        else if (idx32)
+            k_ref_step<false, uint32_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
+                                                                     h->d_macro);
         else
-            k_ref_step<false><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+            k_ref_step<false, size_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
+                                                                   h->d_macro);
         return cudaGetLastError();
     }
     // auto = the fastest variant measured on GB300: one cell per thread for FP32 and FP64
