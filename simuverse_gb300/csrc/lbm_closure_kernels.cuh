@@ -47,6 +47,17 @@ __device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const unsigned* row) {
                  : "r"(a));
 }
 
+// 16-byte global -> shared copy that bypasses the registers (cp.async); with full == false the
+// destination is zero-filled and nothing is read
+__device__ __forceinline__ void cp_async16(unsigned* dst, const void* src, bool full) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = full ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 __device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const unsigned*>(&v);
@@ -86,7 +97,6 @@ __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16
     for (int i = tid; i < SR * ROWC * VPC; i += 32 * CONV_WARPS) {
         const int v = i % VPC, cell = (i / VPC) % ROWC, r = i / (VPC * ROWC);
         int gy = y0 + r - 1, gx = xs + cell - 1;
-        uint4 val = make_uint4(0u, 0u, 0u, 0u);
         bool ok = true;
         if (PERIODIC) {  // staged rows run from -1 to H + CONV_ROWS, which may exceed 2 H
             gy = ((gy % H) + H) % H;
@@ -94,14 +104,16 @@ __global__ void __launch_bounds__(32 * CONV_WARPS) k_conv3x3(const __nv_bfloat16
         } else {
             ok = gy >= 0 && gy < H && gx >= 0 && gx < W;
         }
-        if (ok) val = *reinterpret_cast<const uint4*>(in + (img_off + (size_t)gy * W + gx) * CIN + v * 8);
-        *reinterpret_cast<uint4*>(sin + (r * ROWC + cell) * CS + v * 4) = val;
+        // asynchronous 16-byte copy; a cell outside the image is filled with zeros (source size 0)
+        const __nv_bfloat16* src = ok ? in + (img_off + (size_t)gy * W + gx) * CIN + v * 8 : in;
+        cp_async16(sin + (r * ROWC + cell) * CS + v * 4, src, ok);
     }
     // stage the weights
     for (int i = tid; i < 9 * COUT * VPC; i += 32 * CONV_WARPS) {
         const int v = i % VPC, row = i / VPC;  // row = tap * COUT + co
-        *reinterpret_cast<uint4*>(sw + row * CS + v * 4) = *reinterpret_cast<const uint4*>(wk + (size_t)row * CIN + v * 8);
+        cp_async16(sw + row * CS + v * 4, wk + (size_t)row * CIN + v * 8, true);
     }
+    cp_async_wait_all();
     __syncthreads();
 
     const int x0 = xs + warp * 16;
