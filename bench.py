@@ -37,14 +37,16 @@ UNIT = "GLUPS"
 
 def workload_params(args):
     return dict(nx=args.nx, ny=args.ny, mode="physics", dtype=args.dtype, scene="channel", tau=0.56,
-                inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0), seed=1234, kernel=args.kernel)
+                inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0), seed=1234, kernel=args.kernel,
+                rounding=args.rounding)
 
 
 def config_dict(args):
     return {"workload": "channel %dx%d %s, Zou-He inlet u=0.05 parabolic, outflow, walls, disks r 8-32 5%% solid, "
                         "tau 0.56, equilibrium start" % (args.nx, args.ny, args.dtype),
             "cells": args.nx * args.ny, "steps_per_bench_step": 1, "l2_flush": "none: working set 1.2 GB > L2",
-            "parallelism": "replicas" if args.gpus > 1 else "single GPU", "kernel": args.kernel}
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU", "kernel": args.kernel,
+            "rounding": args.rounding}
 
 
 def dist_env():
@@ -333,8 +335,9 @@ def run_precision(args):
     base = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
                 seed=1234)
     for dtype in () if args.skip_glups else ("f32", "f16", "bf16"):
-        for kernel in ("cell", "vec2", "vec4", "bulk") + (("tiled",) if dtype != "f32" else ()):
-            sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel, **base)
+        for kernel in ("cell", "vec2", "vec4", "bulk") + (("tiled", "tiled+sr") if dtype != "f32" else ()):
+            rounding = "stochastic" if kernel.endswith("+sr") else "nearest"
+            sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel.split("+")[0], rounding=rounding, **base)
             sim.set_stream(stream.cuda_stream)
             sim.step(args.warmup)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -352,7 +355,10 @@ def run_precision(args):
     checkpoints = sorted(set([c for c in args.checkpoints if c < args.steps] + [args.steps]))
     for tau in args.taus:
         coll = args.error_collision if args.error_collision != "auto" else ("kbc" if tau < 0.55 else "bgk")
-        sims = {d: FluidSimulator(nx, ny, dtype=d, tau=tau, collision=coll, **base) for d in ("f64", "f32", "f16", "bf16")}
+        # f16sr / bf16sr: the same storage with stochastic rounding
+        forms = ("f64", "f32", "f16", "bf16", "f16sr", "bf16sr")
+        sims = {d: FluidSimulator(nx, ny, dtype=d[:-2] if d.endswith("sr") else d, tau=tau, collision=coll,
+                                  rounding="stochastic" if d.endswith("sr") else "nearest", **base) for d in forms}
         m0 = {d: s.conservation()[0] for d, s in sims.items()}
         rows, done = [], 0
         for cp in checkpoints:
@@ -362,7 +368,7 @@ def run_precision(args):
             ref = sims["f64"]
             row = {"step": cp, "fp64_mass_change": (ref.conservation()[0] - m0["f64"]) / m0["f64"],
                    "fp64_nonfinite": ref.nonfinite_count()}
-            for d in ("f32", "f16", "bf16"):
+            for d in forms[1:]:
                 err = sims[d].macro_error(ref)
                 row[d] = {"rel_l2_rho": err[0], "rel_l2_u": err[1], "max_du": err[2],
                           "mass_change": (sims[d].conservation()[0] - m0[d]) / m0[d],
@@ -563,6 +569,8 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2", "tiled"])
+    ap.add_argument("--rounding", default="nearest", choices=["nearest", "stochastic"],
+                    help="rounding of 16-bit population stores")
     ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch", "closure", "view"])
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snapshots", type=int, default=125)

@@ -98,6 +98,17 @@ extern "C" {
                                         moments at a per-cell entropic rate; stable for under-
                                         resolved turbulence near tau = 1/2 */
 
+/* physics mode, FP16 / BF16 storage: rounding of the stored populations */
+#define LBM_ROUNDING_NEAREST 0     /* round to nearest even */
+#define LBM_ROUNDING_STOCHASTIC 1  /* stochastic rounding: a value between two stored neighbours is
+                                      stored as the upper one with probability equal to its
+                                      fractional position, so rounding errors have zero mean and
+                                      slow gradients below the 16-bit spacing are kept on average;
+                                      random bits from a hash of cell, step counter and seed
+                                      (reproducible).  Runs on LBM_KERNEL_TILED and
+                                      LBM_KERNEL_CELL (AUTO picks the tiled kernel where it
+                                      applies, else the one-cell kernel). */
+
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */
 #define LBM_SCENE_CAVITY 1     /* lattice.rs:52-61 (reference); moving-lid box (physics) */
@@ -139,7 +150,8 @@ typedef struct lbm_params {
                                 0: only on the last step of each lbm_step call */
     int32_t kernel;          /* LBM_KERNEL_*: step kernel variant (results agree to rounding) */
     int32_t collision;       /* physics mode: LBM_COLLISION_* */
-    int32_t reserved[4];
+    int32_t rounding;        /* LBM_ROUNDING_* (16-bit storage; NEAREST otherwise) */
+    int32_t reserved[3];
 } lbm_params;
 
 typedef struct lbm_handle lbm_handle;

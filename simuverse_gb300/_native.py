@@ -28,6 +28,7 @@ DTYPES = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4}
 KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3, "vec2": 4, "tiled": 5}
 COLLISIONS = {"bgk": 0, "regularized": 1, "mrt": 2, "kbc": 3}
+ROUNDINGS = {"nearest": 0, "stochastic": 1}
 BULK, BOUNDARY, INLET, OBSTACLE, OUTLET, EXTERNAL_FORCE, GHOST = 1, 2, 3, 4, 5, 6, 7
 
 # LatticeInfo (simuverse/src/fluid/lattice.rs:5-13)
@@ -42,7 +43,8 @@ class LbmParams(ctypes.Structure):
         ("solid_fraction", ctypes.c_float), ("disk_rmin", ctypes.c_float), ("disk_rmax", ctypes.c_float),
         ("seed", ctypes.c_uint64),
         ("pixel_size", ctypes.c_int32), ("macro_every_step", ctypes.c_int32),
-        ("kernel", ctypes.c_int32), ("collision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
+        ("kernel", ctypes.c_int32), ("collision", ctypes.c_int32), ("rounding", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 

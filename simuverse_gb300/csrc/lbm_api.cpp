@@ -236,6 +236,14 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "unknown collision %d", p.collision);
     if (p.collision != LBM_COLLISION_BGK && p.mode != LBM_MODE_PHYSICS)
         return fail(LBM_ERR_ARG, "reference mode is BGK only");
+    if (p.rounding != LBM_ROUNDING_NEAREST && p.rounding != LBM_ROUNDING_STOCHASTIC)
+        return fail(LBM_ERR_ARG, "unknown rounding %d", p.rounding);
+    if (p.rounding == LBM_ROUNDING_STOCHASTIC) {
+        if (p.mode != LBM_MODE_PHYSICS || (p.dtype != LBM_DTYPE_F16 && p.dtype != LBM_DTYPE_BF16))
+            return fail(LBM_ERR_ARG, "stochastic rounding applies to physics-mode FP16 / BF16 storage");
+        if (p.kernel != LBM_KERNEL_AUTO && p.kernel != LBM_KERNEL_TILED && p.kernel != LBM_KERNEL_CELL)
+            return fail(LBM_ERR_ARG, "stochastic rounding runs on the tiled and one-cell kernels");
+    }
     if (p.kernel == LBM_KERNEL_VEC2 && (p.mode != LBM_MODE_PHYSICS || p.nx % 2 != 0))
         return fail(LBM_ERR_ARG, "the two-cell kernel needs physics mode and nx %% 2 == 0");
     if (p.kernel == LBM_KERNEL_VEC4 && (p.mode != LBM_MODE_PHYSICS || p.nx % 4 != 0))

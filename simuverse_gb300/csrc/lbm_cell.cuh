@@ -53,7 +53,8 @@ __device__ __forceinline__ void phys_collide(R (&d)[9], int m, unsigned fl, size
             in.block_iter = in.block_iter - 1;
             if (in.block_iter == 0) {
                 in.material = LBM_BULK;
-                flags[c] = (uint16_t)((fl & ~FL_MAT_MASK) | LBM_BULK);
+                const unsigned nf = (fl & ~FL_MAT_MASK) | LBM_BULK;
+                flags[c] = (uint16_t)(nf | plain_bit(nf));
             }
             info[c] = in;
         }
@@ -235,39 +236,44 @@ __device__ __forceinline__ void bgk_plain_fast(const float (&d)[9], float omega,
                                                float& rho_out, float& ux_out, float& uy_out) {
     const float s13 = d[1] + d[3], s24 = d[2] + d[4], s57 = d[5] + d[7], s68 = d[6] + d[8];
     const float drho = d[0] + ((s13 + s24) + (s57 + s68));
-    const float d86 = d[8] - d[6];
-    const float jx = (d[1] - d[3]) + ((d[5] - d[7]) + d86);
-    const float jy = (d[4] - d[2]) + ((d[7] - d[5]) + d86);
+    const float d86 = d[8] - d[6], d57 = d[5] - d[7];
+    const float jx = (d[1] - d[3]) + (d57 + d86);
+    const float jy = (d[4] - d[2]) + (d86 - d57);
     const float rho = U + drho;
     const float inv = __fdividef(1.0f, rho);
     const float ux = jx * inv, uy = jy * inv;
-    const float usq = 1.5f * (ux * ux + uy * uy);
+    const float uxx = ux * ux, uyy = uy * uy;
+    // t0 = drho - 1.5 rho u.u is the isotropic part of every equilibrium deviation; the pair
+    // (j, inv j) shares w_j (t0 + 4.5 rho (e_j.u)^2) and differs by -+ 3 w_j rho e_j.u
+    const float t0 = drho - rho * (1.5f * (uxx + uyy));
     const float om1 = 1.0f - omega;
     const float w1 = omega * PW<float>(1), w5 = omega * PW<float>(5);
+    const float a1 = w1 * t0, a5 = w5 * t0;
     const float r1 = rho * (3.0f * w1), r5 = rho * (3.0f * w5);
+    const float q1 = rho * (4.5f * w1), q5 = rho * (4.5f * w5);
     {
-        const float sym = w1 * (drho + rho * (4.5f * ux * ux - usq)), asy = r1 * ux;
-        o[1] = om1 * d[1] + (sym + asy);
-        o[3] = om1 * d[3] + (sym - asy);
+        const float sym = q1 * uxx + a1;
+        o[1] = om1 * d[1] + (r1 * ux + sym);
+        o[3] = om1 * d[3] + (sym - r1 * ux);
     }
     {
-        const float sym = w1 * (drho + rho * (4.5f * uy * uy - usq)), asy = r1 * uy;
-        o[4] = om1 * d[4] + (sym + asy);
-        o[2] = om1 * d[2] + (sym - asy);
+        const float sym = q1 * uyy + a1;
+        o[4] = om1 * d[4] + (r1 * uy + sym);
+        o[2] = om1 * d[2] + (sym - r1 * uy);
     }
     {
         const float eu = ux + uy;
-        const float sym = w5 * (drho + rho * (4.5f * eu * eu - usq)), asy = r5 * eu;
-        o[8] = om1 * d[8] + (sym + asy);
-        o[6] = om1 * d[6] + (sym - asy);
+        const float sym = q5 * (eu * eu) + a5;
+        o[8] = om1 * d[8] + (r5 * eu + sym);
+        o[6] = om1 * d[6] + (sym - r5 * eu);
     }
     {
         const float eu = ux - uy;
-        const float sym = w5 * (drho + rho * (4.5f * eu * eu - usq)), asy = r5 * eu;
-        o[5] = om1 * d[5] + (sym + asy);
-        o[7] = om1 * d[7] + (sym - asy);
+        const float sym = q5 * (eu * eu) + a5;
+        o[5] = om1 * d[5] + (r5 * eu + sym);
+        o[7] = om1 * d[7] + (sym - r5 * eu);
     }
-    o[0] = om1 * d[0] + (omega * PW<float>(0)) * (drho - rho * usq);
+    o[0] = om1 * d[0] + (omega * PW<float>(0)) * t0;
     rho_out = rho * (1.0f / U);
     ux_out = ux;
     uy_out = uy;
@@ -275,11 +281,12 @@ __device__ __forceinline__ void bgk_plain_fast(const float (&d)[9], float omega,
 
 // One cell (x, y) of a lattice of nx x ny cells whose rows are `pitch` elements apart
 // (pitch >= nx; the single-lattice kernel passes pitch = nx).
-template <class ST, bool MACRO, int COLL = LBM_COLLISION_BGK>
+// SR: stochastic rounding of the stores with the step's `seed` (lbm_common.cuh).
+template <class ST, bool MACRO, int COLL = LBM_COLLISION_BGK, bool SR = false>
 __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                  typename ST::R omega, int x, int y, int nx, int pitch, int ny,
-                                                 float* __restrict__ macro) {
+                                                 float* __restrict__ macro, uint32_t seed = 0) {
     using R = typename ST::R;
     const size_t N = (size_t)pitch * ny;
     const unsigned c = (unsigned)y * (unsigned)pitch + (unsigned)x;  // cells < 2^31
@@ -324,8 +331,14 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
     R o[9], rho, ux, uy;
     phys_collide<R, COLL>(d, m, fl, c, flags, info, omega, o, rho, ux, uy, R(ST::UNIT));
     if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
+    if (SR) {
+        const uint32_t q = sr_hash(c ^ seed);
 #pragma unroll
-    for (int j = 0; j < 9; ++j) ST::stu(B + (size_t)j * N + c, o[j]);
+        for (int j = 0; j < 9; ++j) ST::stu_sr(B + (size_t)j * N + c, o[j], q * sr_mul(j));
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) ST::stu(B + (size_t)j * N + c, o[j]);
+    }
 }
 
 }  // namespace lbm

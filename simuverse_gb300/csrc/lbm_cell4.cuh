@@ -96,6 +96,7 @@ struct Vec2<StoreF32> {
     __device__ __forceinline__ static void st(float* p, const float (&r)[2]) {
         *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
     }
+    __device__ __forceinline__ static void st_sr(float* p, const float (&r)[2], uint32_t, uint32_t) { st(p, r); }
 };
 template <>
 struct Vec2<StoreF64> {
@@ -106,6 +107,7 @@ struct Vec2<StoreF64> {
     __device__ __forceinline__ static void st(double* p, const double (&r)[2]) {
         *reinterpret_cast<double2*>(p) = make_double2(r[0], r[1]);
     }
+    __device__ __forceinline__ static void st_sr(double* p, const double (&r)[2], uint32_t, uint32_t) { st(p, r); }
 };
 template <>
 struct Vec2<StoreF16> {
@@ -118,6 +120,11 @@ struct Vec2<StoreF16> {
         const __half2 a = __floats2half2_rn(r[0], r[1]);
         *reinterpret_cast<unsigned*>(p) = *reinterpret_cast<const unsigned*>(&a);
     }
+    // stochastic rounding with random words q0, q1 (lbm_common.cuh)
+    __device__ __forceinline__ static void st_sr(__half* p, const float (&r)[2], uint32_t q0, uint32_t q1) {
+        *reinterpret_cast<unsigned*>(p) = pack_half2_rz(sr_dither<StoreF16::SR_DROP>(r[0], q0),
+                                                        sr_dither<StoreF16::SR_DROP>(r[1], q1));
+    }
 };
 template <>
 struct Vec2<StoreBF16> {
@@ -129,6 +136,10 @@ struct Vec2<StoreBF16> {
     __device__ __forceinline__ static void st(__nv_bfloat16* p, const float (&r)[2]) {
         const __nv_bfloat162 a = __floats2bfloat162_rn(r[0], r[1]);
         *reinterpret_cast<unsigned*>(p) = *reinterpret_cast<const unsigned*>(&a);
+    }
+    __device__ __forceinline__ static void st_sr(__nv_bfloat16* p, const float (&r)[2], uint32_t q0, uint32_t q1) {
+        *reinterpret_cast<unsigned*>(p) = pack_bf162_rz(sr_dither<StoreBF16::SR_DROP>(r[0], q0),
+                                                        sr_dither<StoreBF16::SR_DROP>(r[1], q1));
     }
 };
 
@@ -204,11 +215,7 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
     // material, no solid pull source) -- no boundary rule to test per cell
     bool plain = true;
 #pragma unroll
-    for (int k = 0; k < CPT; ++k) {
-        const unsigned mat = fl[k] & FL_MAT_MASK;
-        plain = plain && (mat == LBM_BULK || mat == LBM_GHOST || mat == 0u) && !(fl[k] & (0x1FFu << FL_DIR_SHIFT)) &&
-                x0 + k < nx;
-    }
+    for (int k = 0; k < CPT; ++k) plain = plain && (fl[k] & FL_PLAIN) && x0 + k < nx;
     const bool fast = __all_sync(0xffffffffu, !active || plain);
     if (!active) return;
 

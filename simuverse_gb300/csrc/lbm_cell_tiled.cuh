@@ -17,10 +17,12 @@
 
 namespace lbm {
 
-template <class ST, bool MACRO>
+// SR: stochastic rounding of the stores with the step's `seed` (lbm_common.cuh)
+template <class ST, bool MACRO, bool SR = false>
 __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
-                                                 float omega, int tx, int y, int nx, int ny, float* __restrict__ macro) {
+                                                 float omega, int tx, int y, int nx, int ny, float* __restrict__ macro,
+                                                 uint32_t seed = 0) {
     using T = typename ST::T;
     using R = float;
     constexpr int W = POP_TILE, TS = 9 * POP_TILE;  // cells per tile, elements per tile
@@ -41,11 +43,9 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
     const uint32_t c0 = (uint32_t)y * nx + x0;  // cell index (flags, info, macro)
 
     unsigned fl[2];
-    {
-        const unsigned q = *reinterpret_cast<const unsigned*>(flags + c0);
-        fl[0] = q & 0xffffu;
-        fl[1] = q >> 16;
-    }
+    const unsigned fq = *reinterpret_cast<const unsigned*>(flags + c0);
+    fl[0] = fq & 0xffffu;
+    fl[1] = fq >> 16;
 
     const T* Pm = A + om;  // every plane of a tile is a compile-time offset from these
     const T* P0 = A + o0;
@@ -72,13 +72,7 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
         }
     }
 
-    bool plain = true;
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const unsigned mat = fl[k] & FL_MAT_MASK;
-        plain = plain && (mat == LBM_BULK || mat == LBM_GHOST || mat == 0u) && !(fl[k] & (0x1FFu << FL_DIR_SHIFT));
-    }
-    const bool fast = __all_sync(0xffffffffu, plain);
+    const bool fast = __all_sync(0xffffffffu, (fq & (FL_PLAIN | FL_PLAIN << 16)) == (FL_PLAIN | FL_PLAIN << 16));
 
     R mr[2], mu[2], mv[2];
     if (fast) {
@@ -137,8 +131,14 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
         }
     }
     T* Q0 = B + o0;
+    if (SR) {
+        const uint32_t q = sr_hash(c0 ^ seed);
 #pragma unroll
-    for (int j = 0; j < 9; ++j) Vec2<ST>::st(Q0 + j * W, d[j]);
+        for (int j = 0; j < 9; ++j) Vec2<ST>::st_sr(Q0 + j * W, d[j], q * sr_mul(2 * j), q * sr_mul(2 * j + 1));
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) Vec2<ST>::st(Q0 + j * W, d[j]);
+    }
     if (MACRO) {
         *reinterpret_cast<float2*>(macro + c0) = make_float2(mr[0], mr[1]);
         *reinterpret_cast<float2*>(macro + N + c0) = make_float2(mu[0], mu[1]);

@@ -41,9 +41,18 @@ __host__ __device__ constexpr R PW(int j) {
 //     reference mode, solid cell: slot k is zeroed (wall-to-wall slot, see lbm_kernels.cu);
 //     physics mode, fluid cell: the pull source of direction k is solid (bounce-back).
 //   bit 13    physics mode: some bounce-back source is a moving wall
+//   bit 14    physics mode: plain fluid (bulk, ghost or code 0, no solid pull source), the
+//             cells the step kernels' warp-uniform fast path takes
 constexpr unsigned FL_MAT_MASK = 15u;
 constexpr int FL_DIR_SHIFT = 4;
 constexpr unsigned FL_MOVING = 1u << 13;
+constexpr unsigned FL_PLAIN = 1u << 14;
+__host__ __device__ constexpr unsigned plain_bit(unsigned fl) {
+    return ((fl & FL_MAT_MASK) == LBM_BULK || (fl & FL_MAT_MASK) == LBM_GHOST || (fl & FL_MAT_MASK) == 0u) &&
+                   !(fl & (0x1FFu << FL_DIR_SHIFT))
+               ? FL_PLAIN
+               : 0u;
+}
 
 __host__ __device__ constexpr bool is_solid(int m) { return m == LBM_BOUNDARY || m == LBM_OBSTACLE; }
 
@@ -65,6 +74,57 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float recip_rn(float a) { return __frcp_rn(a); }
 __device__ __forceinline__ double recip_rn(double a) { return __drcp_rn(a); }
 
+// ---- stochastic rounding of 16-bit stores (LBM_ROUNDING_STOCHASTIC) ---------------
+// A value v between two neighbouring stored values lo < v < hi is stored as hi with
+// probability (v - lo) / (hi - lo), so the rounding error has zero mean: a field that changes
+// by less than the stored spacing from one cell or step to the next (the pressure gradient of
+// an open channel) is kept on average instead of being rounded away, the stagnation of
+// round-to-nearest (Connolly, Higham & Mary, SIAM J. Sci. Comput. 43 (2021) A566).  The store
+// adds a uniform random integer below the stored precision to the FP32 bit pattern (the
+// significand bits that the conversion drops: SR_DROP) and converts rounding toward zero; the
+// pattern's low 31 bits are the magnitude, so both signs round alike.  Where the 16-bit image
+// is subnormal (FP16 stored magnitudes below 2^-14) more bits are dropped and the rounding
+// keeps a bias toward zero of at most that spacing.
+//
+// Random bits: one hash per thread and step, sr_hash(cell ^ seed), the "lowbias32" integer
+// hash of C. Wellons' hash-prospector (2018); the value j of a thread takes the top SR_DROP
+// bits of hash * sr_mul(j) (odd multipliers, so every value's bits are uniform).  The host
+// derives seed from the step counter (sr_seed): runs are reproducible.
+__host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__host__ __device__ constexpr uint32_t sr_mul(int i) {
+    return (((0x9E3779B9u * (uint32_t)(i + 1)) ^ ((0x9E3779B9u * (uint32_t)(i + 1)) >> 15)) * 0x2C1B3C6Du) | 1u;
+}
+// seed of step `step` of a handle whose channel seed is `seed` (splitmix64 finaliser)
+inline uint32_t sr_seed(uint64_t step, uint64_t seed) {
+    uint64_t z = step + 0x9E3779B97F4A7C15ull * (seed + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return (uint32_t)((z ^ (z >> 31)) >> 32);
+}
+// v with `r`'s top DROP bits added to its pattern (the conversion that follows truncates)
+template <int DROP>
+__device__ __forceinline__ float sr_dither(float v, uint32_t r) {
+    return __uint_as_float(__float_as_uint(v) + (r >> (32 - DROP)));
+}
+// two FP32 values to packed 16-bit (element 0 in the low half), rounding toward zero
+__device__ __forceinline__ unsigned pack_half2_rz(float a0, float a1) {
+    unsigned d;
+    asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(a1), "f"(a0));
+    return d;
+}
+__device__ __forceinline__ unsigned pack_bf162_rz(float a0, float a1) {
+    unsigned d;
+    asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(a1), "f"(a0));
+    return d;
+}
+
 // ---- population storage formats ------------------------------------------------
 // R: arithmetic type; T: stored type.  Physics-mode storage holds d = f - w (shifted
 // deviation); FP16 additionally scales by 2^10 so that small deviations stay normal.
@@ -77,6 +137,7 @@ struct StoreF32 {
     __device__ __forceinline__ static void st(T* p, R v) { *p = v; }
     __device__ __forceinline__ static R ldu(const T* p) { return __ldg(p); }
     __device__ __forceinline__ static void stu(T* p, R v) { *p = v; }
+    __device__ __forceinline__ static void stu_sr(T* p, R v, uint32_t) { *p = v; }  // no rounding
     __host__ __device__ static R to_r(T v) { return v; }
     __host__ __device__ static T from_r(R v) { return v; }
 };
@@ -89,6 +150,7 @@ struct StoreF64 {
     __device__ __forceinline__ static void st(T* p, R v) { *p = v; }
     __device__ __forceinline__ static R ldu(const T* p) { return __ldg(p); }
     __device__ __forceinline__ static void stu(T* p, R v) { *p = v; }
+    __device__ __forceinline__ static void stu_sr(T* p, R v, uint32_t) { *p = v; }  // no rounding
     __host__ __device__ static R to_r(T v) { return v; }
     __host__ __device__ static T from_r(R v) { return v; }
 };
@@ -105,6 +167,10 @@ struct StoreF16 {
     __device__ __forceinline__ static void st(T* p, R v) { *p = __float2half_rn(v * F16_SCALE); }
     __device__ __forceinline__ static R ldu(const T* p) { return __half2float(__ldg(p)); }
     __device__ __forceinline__ static void stu(T* p, R v) { *p = __float2half_rn(v); }
+    static constexpr int SR_DROP = 13;  // FP32 significand bits below FP16's
+    __device__ __forceinline__ static void stu_sr(T* p, R v, uint32_t r) {
+        *p = __float2half_rz(sr_dither<SR_DROP>(v, r));
+    }
     __host__ __device__ static R to_r(T v) { return __half2float(v) * F16_INV_SCALE; }
     __host__ __device__ static T from_r(R v) { return __float2half_rn(v * F16_SCALE); }
 };
@@ -117,6 +183,10 @@ struct StoreBF16 {
     __device__ __forceinline__ static void st(T* p, R v) { *p = __float2bfloat16_rn(v); }
     __device__ __forceinline__ static R ldu(const T* p) { return __bfloat162float(__ldg(p)); }
     __device__ __forceinline__ static void stu(T* p, R v) { *p = __float2bfloat16_rn(v); }
+    static constexpr int SR_DROP = 16;  // FP32 significand bits below BF16's
+    __device__ __forceinline__ static void stu_sr(T* p, R v, uint32_t r) {
+        *p = __float2bfloat16_rz(sr_dither<SR_DROP>(v, r));
+    }
     __host__ __device__ static R to_r(T v) { return __bfloat162float(v); }
     __host__ __device__ static T from_r(R v) { return __float2bfloat16_rn(v); }
 };

@@ -65,6 +65,7 @@ __global__ void k_build_flags(const lbm_lattice_info* __restrict__ info, uint16_
                 }
             }
         }
+        fl |= plain_bit(fl);
     }
     flags[c] = (uint16_t)fl;
 }
@@ -245,14 +246,16 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
 // physics-mode step (cell update in lbm_cell.cuh)
 // ------------------------------------------------------------------------------------
 // BGK and regularised fit 32 registers (full occupancy); MRT and KBC get 48
-template <class ST, bool MACRO, int COLL>
+// (SR: stochastic rounding of 16-bit stores, seed from the step counter)
+template <class ST, bool MACRO, int COLL, bool SR>
 __global__ void __launch_bounds__(TPB, (COLL == LBM_COLLISION_MRT || COLL == LBM_COLLISION_KBC) ? 10 : 16) k_phys_step(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
-                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro) {
+                                                   typename ST::R omega, int nx, int ny, float* __restrict__ macro,
+                                                   uint32_t seed) {
     const int x = blockIdx.x * TPB + threadIdx.x;
     const int y = blockIdx.y;
     if (x >= nx) return;
-    phys_cell_update<ST, MACRO, COLL>(A, B, flags, info, omega, x, y, nx, nx, ny, macro);
+    phys_cell_update<ST, MACRO, COLL, SR>(A, B, flags, info, omega, x, y, nx, nx, ny, macro, seed);
 }
 
 // ------------------------------------------------------------------------------------
@@ -547,8 +550,15 @@ static cudaError_t phys_step_c(lbm_handle* h, cudaStream_t s) {
     using T = typename ST::T;
     using R = typename ST::R;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
-    k_phys_step<ST, MACRO, COLL><<<cell_grid(h), TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
-                                                              h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
+    // stochastic rounding exists for 16-bit storage only (validated at create)
+    constexpr bool SIXTEEN = ST::dtype == LBM_DTYPE_F16 || ST::dtype == LBM_DTYPE_BF16;
+    if (SIXTEEN && h->p.rounding == LBM_ROUNDING_STOCHASTIC)
+        k_phys_step<ST, MACRO, COLL, SIXTEEN><<<cell_grid(h), TPB, 0, s>>>(
+            (const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro,
+            sr_seed(h->steps, h->p.seed));
+    else
+        k_phys_step<ST, MACRO, COLL, false><<<cell_grid(h), TPB, 0, s>>>(
+            (const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro, 0u);
     return cudaGetLastError();
 }
 
@@ -598,7 +608,7 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_AUTO && (h->p.dtype == LBM_DTYPE_F16 || h->p.dtype == LBM_DTYPE_BF16) &&
-        h->nx % 2 == 0)
+        h->nx % 2 == 0 && h->p.rounding == LBM_ROUNDING_NEAREST)
         return launch_phys_step_vec2(h, write_macro, s);
     switch (h->p.dtype) {
         case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);

@@ -78,18 +78,18 @@ static cudaError_t phys_step_v4_t(lbm_handle* h, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// tiled 16-bit layout: one warp per 64-cell tile, consecutive warps along a row
-template <class ST, bool MACRO>
+// tiled 16-bit layout: one warp per 64-cell tile, the warps of a block on consecutive tiles
+// of row blockIdx.y (SR: stochastic rounding of the stores, seed from the step counter)
+template <class ST, bool MACRO, bool SR>
 __global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_tiled(const typename ST::T* __restrict__ A,
                                                                  typename ST::T* __restrict__ B,
                                                                  uint16_t* __restrict__ flags,
                                                                  lbm_lattice_info* __restrict__ info, float omega,
-                                                                 int nx, int ny, float* __restrict__ macro) {
-    const int warp = (int)((blockIdx.x * VEC_TPB + threadIdx.x) >> 5);
-    const int tpr = nx / POP_TILE;
-    if (warp >= tpr * ny) return;  // whole warps
-    const int y = warp / tpr;
-    phys_tile_update<ST, MACRO>(A, B, flags, info, omega, warp - y * tpr, y, nx, ny, macro);
+                                                                 int nx, int ny, float* __restrict__ macro,
+                                                                 uint32_t seed) {
+    const int tx = (int)((blockIdx.x * VEC_TPB + threadIdx.x) >> 5);
+    if (tx >= nx / POP_TILE) return;  // whole warps
+    phys_tile_update<ST, MACRO, SR>(A, B, flags, info, omega, tx, (int)blockIdx.y, nx, ny, macro, seed);
 }
 
 bool tiled_layout_eligible(const lbm_params& p) {
@@ -97,20 +97,26 @@ bool tiled_layout_eligible(const lbm_params& p) {
            p.collision == LBM_COLLISION_BGK && p.nx % POP_TILE == 0 && (size_t)9 * p.nx * p.ny < ((size_t)1 << 32);
 }
 
-template <class ST, bool MACRO>
+template <class ST, bool MACRO, bool SR>
 static cudaError_t phys_step_tiled_t(lbm_handle* h, cudaStream_t s) {
     using T = typename ST::T;
-    const size_t threads = (size_t)(h->nx / POP_TILE) * h->ny * 32;
-    const unsigned blocks = (unsigned)((threads + VEC_TPB - 1) / VEC_TPB);
-    k_phys_step_tiled<ST, MACRO><<<blocks, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
-                                                            h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+    const dim3 grid((unsigned)((h->nx / POP_TILE * 32 + VEC_TPB - 1) / VEC_TPB), (unsigned)h->ny);
+    k_phys_step_tiled<ST, MACRO, SR><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
+                                                                h->d_flags, h->d_info, h->omega, h->nx, h->ny,
+                                                                h->d_macro, sr_seed(h->steps, h->p.seed));
     return cudaGetLastError();
 }
 
+template <class ST>
+static cudaError_t phys_step_tiled_r(lbm_handle* h, bool write_macro, cudaStream_t s) {
+    if (h->p.rounding == LBM_ROUNDING_STOCHASTIC)
+        return write_macro ? phys_step_tiled_t<ST, true, true>(h, s) : phys_step_tiled_t<ST, false, true>(h, s);
+    return write_macro ? phys_step_tiled_t<ST, true, false>(h, s) : phys_step_tiled_t<ST, false, false>(h, s);
+}
+
 cudaError_t launch_phys_step_tiled(lbm_handle* h, bool write_macro, cudaStream_t s) {
-    if (h->p.dtype == LBM_DTYPE_F16)
-        return write_macro ? phys_step_tiled_t<StoreF16, true>(h, s) : phys_step_tiled_t<StoreF16, false>(h, s);
-    return write_macro ? phys_step_tiled_t<StoreBF16, true>(h, s) : phys_step_tiled_t<StoreBF16, false>(h, s);
+    if (h->p.dtype == LBM_DTYPE_F16) return phys_step_tiled_r<StoreF16>(h, write_macro, s);
+    return phys_step_tiled_r<StoreBF16>(h, write_macro, s);
 }
 
 bool vec_step_supported(const lbm_handle* h) { return h->p.mode == LBM_MODE_PHYSICS && (h->nx % 4) == 0; }

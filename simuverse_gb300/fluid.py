@@ -32,7 +32,8 @@ class FluidSimulator:
                  scene: str = "poiseuille", tau: float = None, viscosity: float = None,
                  lid_speed: float = None, inlet_speed: float = None, solid_fraction: float = 0.05,
                  disk_radius=(8.0, 32.0), seed: int = 0, pixel_size: int = 2,
-                 macro_every_step: bool = False, kernel: str = "auto", collision: str = "bgk"):
+                 macro_every_step: bool = False, kernel: str = "auto", collision: str = "bgk",
+                 rounding: str = "nearest"):
         lib = nat.load()
         p = nat.LbmParams()
         lib.lbm_params_default(ctypes.byref(p))
@@ -55,6 +56,7 @@ class FluidSimulator:
         p.macro_every_step = 1 if macro_every_step else 0
         p.kernel = nat.KERNELS[kernel]
         p.collision = nat.COLLISIONS[collision]
+        p.rounding = nat.ROUNDINGS[rounding]
         h = ctypes.c_void_p()
         nat.check(lib.lbm_create(ctypes.byref(p), ctypes.byref(h)))
         self._lib = lib
@@ -62,6 +64,7 @@ class FluidSimulator:
         self.nx, self.ny = int(nx), int(ny)
         self.N = self.nx * self.ny
         self.mode, self.dtype, self.scene = mode, dtype, scene
+        self.rounding = rounding
         self.pixel_size = int(pixel_size)
 
     # ------------------------------------------------------------------ lifetime

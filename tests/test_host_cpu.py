@@ -52,6 +52,27 @@ def test_create_rejects_bad_params(native, field, value):
     assert len(native.lbm_last_error()) > 0
 
 
+@pytest.mark.parametrize("mode,dtype,kernel,rounding", [
+    (0, 0, 0, 1),  # reference mode
+    (1, 0, 0, 1),  # physics FP32: nothing to round
+    (1, 1, 0, 1),  # physics FP64
+    (1, 2, 4, 1),  # FP16 on the two-cell SoA kernel
+    (1, 3, 2, 1),  # BF16 on the four-cell kernel
+    (1, 2, 0, 7),  # unknown rounding
+])
+def test_create_rejects_bad_rounding(native, mode, dtype, kernel, rounding):
+    from simuverse_gb300 import _native as nat
+
+    p = nat.LbmParams()
+    native.lbm_params_default(ctypes.byref(p))
+    p.nx, p.ny, p.mode, p.dtype, p.kernel, p.rounding = 128, 64, mode, dtype, kernel, rounding
+    p.scene = nat.SCENES["periodic"] if mode == 1 else 0
+    h = ctypes.c_void_p()
+    assert native.lbm_create(ctypes.byref(p), ctypes.byref(h)) == nat.LBM_ERR_ARG
+    assert h.value is None
+    assert "round" in native.lbm_last_error().decode()
+
+
 def test_null_handles_are_errors(native):
     from simuverse_gb300 import _native as nat
 
