@@ -335,7 +335,7 @@ def run_precision(args):
     base = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
                 seed=1234)
     for dtype in () if args.skip_glups else ("f32", "f16", "bf16"):
-        for kernel in ("cell", "vec2", "vec4", "bulk") + (("tiled", "tiled+sr") if dtype != "f32" else ()):
+        for kernel in ("cell", "vec2", "vec4", "bulk") + (("tiled", "tiled+sr", "vec2+sr") if dtype != "f32" else ()):
             rounding = "stochastic" if kernel.endswith("+sr") else "nearest"
             sim = FluidSimulator(nx, ny, dtype=dtype, tau=0.6, kernel=kernel.split("+")[0], rounding=rounding, **base)
             sim.set_stream(stream.cuda_stream)

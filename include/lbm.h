@@ -105,9 +105,8 @@ extern "C" {
                                       fractional position, so rounding errors have zero mean and
                                       slow gradients below the 16-bit spacing are kept on average;
                                       random bits from a hash of cell, step counter and seed
-                                      (reproducible).  Runs on LBM_KERNEL_TILED and
-                                      LBM_KERNEL_CELL (AUTO picks the tiled kernel where it
-                                      applies, else the one-cell kernel). */
+                                      (reproducible).  Runs on LBM_KERNEL_TILED, _VEC2 and
+                                      _CELL (AUTO picks as for round-to-nearest). */
 
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */

@@ -241,8 +241,9 @@ int validate_params(const lbm_params& p) {
     if (p.rounding == LBM_ROUNDING_STOCHASTIC) {
         if (p.mode != LBM_MODE_PHYSICS || (p.dtype != LBM_DTYPE_F16 && p.dtype != LBM_DTYPE_BF16))
             return fail(LBM_ERR_ARG, "stochastic rounding applies to physics-mode FP16 / BF16 storage");
-        if (p.kernel != LBM_KERNEL_AUTO && p.kernel != LBM_KERNEL_TILED && p.kernel != LBM_KERNEL_CELL)
-            return fail(LBM_ERR_ARG, "stochastic rounding runs on the tiled and one-cell kernels");
+        if (p.kernel != LBM_KERNEL_AUTO && p.kernel != LBM_KERNEL_TILED && p.kernel != LBM_KERNEL_VEC2 &&
+            p.kernel != LBM_KERNEL_CELL)
+            return fail(LBM_ERR_ARG, "stochastic rounding runs on the tiled, two-cell and one-cell kernels");
     }
     if (p.kernel == LBM_KERNEL_VEC2 && (p.mode != LBM_MODE_PHYSICS || p.nx % 2 != 0))
         return fail(LBM_ERR_ARG, "the two-cell kernel needs physics mode and nx %% 2 == 0");

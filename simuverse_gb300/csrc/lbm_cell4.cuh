@@ -152,11 +152,13 @@ struct VecN<ST, 2> : Vec2<ST> {};
 
 // IDX: the integer type of element offsets (uint32_t when 9 * pitch * ny < 2^32, which saves
 // the 64-bit address arithmetic of every plane access; size_t otherwise)
-template <class ST, bool MACRO, int CPT = 4, class IDX = size_t>
+// SR: stochastic rounding of the stores with the step's `seed` (two cells per thread only)
+template <class ST, bool MACRO, int CPT = 4, class IDX = size_t, bool SR = false>
 __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                    uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                    typename ST::R omega, int x0, int y, int nx, int pitch, int ny,
-                                                   bool active, float* __restrict__ macro) {
+                                                   bool active, float* __restrict__ macro, uint32_t seed = 0) {
+    static_assert(!SR || CPT == 2, "stochastic rounding runs on the two-cell form");
     using R = typename ST::R;
     using T = typename ST::T;
     const int lane = threadIdx.x & 31;
@@ -279,8 +281,15 @@ __device__ __forceinline__ void phys_cells4_update(const typename ST::T* __restr
         for (int j = 0; j < 9; ++j) d[j][k] = o[j];
     }
     }
+    if constexpr (SR) {
+        const uint32_t q = sr_hash((uint32_t)(r0 + (IDX)x0) ^ seed);
 #pragma unroll
-    for (int j = 0; j < 9; ++j) VecN<ST, CPT>::st(B + ((IDX)j * N + r0 + (IDX)x0), d[j]);
+        for (int j = 0; j < 9; ++j)
+            Vec2<ST>::st_sr(B + ((IDX)j * N + r0 + (IDX)x0), d[j], q * sr_mul(2 * j), q * sr_mul(2 * j + 1));
+    } else {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) VecN<ST, CPT>::st(B + ((IDX)j * N + r0 + (IDX)x0), d[j]);
+    }
     if (MACRO) {
 #pragma unroll
         for (int k = 0; k < CPT; ++k) {

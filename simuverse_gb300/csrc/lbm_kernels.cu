@@ -608,7 +608,7 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_AUTO && (h->p.dtype == LBM_DTYPE_F16 || h->p.dtype == LBM_DTYPE_BF16) &&
-        h->nx % 2 == 0 && h->p.rounding == LBM_ROUNDING_NEAREST)
+        h->nx % 2 == 0)
         return launch_phys_step_vec2(h, write_macro, s);
     switch (h->p.dtype) {
         case LBM_DTYPE_F32: return write_macro ? phys_step_t<StoreF32, true>(h, s) : phys_step_t<StoreF32, false>(h, s);

@@ -28,30 +28,40 @@ static inline bool idx32_ok(const lbm_handle* h) { return (size_t)9 * h->N < ((s
 // two cells per thread: one 32-bit access per plane for FP16 / BF16 (threads that walk
 // several rows, amortising the column set-up, measured slower: register spills at 48
 // registers, or lower occupancy at 64)
-template <class ST, bool MACRO, class IDX>
+template <class ST, bool MACRO, class IDX, bool SR>
 __global__ void __launch_bounds__(VEC_TPB, 10) k_phys_step_v2(const typename ST::T* __restrict__ A,
                                                               typename ST::T* __restrict__ B,
                                                               uint16_t* __restrict__ flags,
                                                               lbm_lattice_info* __restrict__ info,
                                                               typename ST::R omega, int nx, int ny,
-                                                              float* __restrict__ macro) {
+                                                              float* __restrict__ macro, uint32_t seed) {
     const int x0 = (blockIdx.x * VEC_TPB + threadIdx.x) * 2;
-    phys_cells4_update<ST, MACRO, 2, IDX>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro);
+    phys_cells4_update<ST, MACRO, 2, IDX, SR>(A, B, flags, info, omega, x0, blockIdx.y, nx, nx, ny, x0 < nx, macro,
+                                              seed);
 }
 
-template <class ST, bool MACRO>
-static cudaError_t phys_step_v2_t(lbm_handle* h, cudaStream_t s) {
+template <class ST, bool MACRO, bool SR>
+static cudaError_t phys_step_v2_s(lbm_handle* h, cudaStream_t s) {
     using T = typename ST::T;
     using R = typename ST::R;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     const dim3 grid((unsigned)((h->nx / 2 + VEC_TPB - 1) / VEC_TPB), (unsigned)h->ny);
+    const uint32_t seed = SR ? sr_seed(h->steps, h->p.seed) : 0u;
     if (idx32_ok(h))
-        k_phys_step_v2<ST, MACRO, uint32_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
-                                                                    h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
+        k_phys_step_v2<ST, MACRO, uint32_t, SR><<<grid, VEC_TPB, 0, s>>>(
+            (const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro, seed);
     else
-        k_phys_step_v2<ST, MACRO, size_t><<<grid, VEC_TPB, 0, s>>>((const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1],
-                                                                  h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro);
+        k_phys_step_v2<ST, MACRO, size_t, SR><<<grid, VEC_TPB, 0, s>>>(
+            (const T*)h->buf[h->cur], (T*)h->buf[h->cur ^ 1], h->d_flags, h->d_info, omega, h->nx, h->ny, h->d_macro, seed);
     return cudaGetLastError();
+}
+
+// stochastic rounding exists for 16-bit storage only (validated at create)
+template <class ST, bool MACRO>
+static cudaError_t phys_step_v2_t(lbm_handle* h, cudaStream_t s) {
+    constexpr bool SIXTEEN = ST::dtype == LBM_DTYPE_F16 || ST::dtype == LBM_DTYPE_BF16;
+    if (SIXTEEN && h->p.rounding == LBM_ROUNDING_STOCHASTIC) return phys_step_v2_s<ST, MACRO, SIXTEEN>(h, s);
+    return phys_step_v2_s<ST, MACRO, false>(h, s);
 }
 
 cudaError_t launch_phys_step_vec2(lbm_handle* h, bool write_macro, cudaStream_t s) {

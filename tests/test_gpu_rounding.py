@@ -65,7 +65,7 @@ def _one_step(dtype, kernel, rounding, nx=128, ny=64, seed=11):
     return x, s
 
 
-@pytest.mark.parametrize("kernel", ["tiled", "cell"])
+@pytest.mark.parametrize("kernel", ["tiled", "vec2", "cell"])
 @pytest.mark.parametrize("dtype", ["f16", "bf16"])
 def test_stochastic_rounding_is_unbiased(gpu, dtype, kernel):
     x, s = _one_step(dtype, kernel, "stochastic")

@@ -56,7 +56,7 @@ def test_create_rejects_bad_params(native, field, value):
     (0, 0, 0, 1),  # reference mode
     (1, 0, 0, 1),  # physics FP32: nothing to round
     (1, 1, 0, 1),  # physics FP64
-    (1, 2, 4, 1),  # FP16 on the two-cell SoA kernel
+    (1, 2, 3, 1),  # FP16 on the bulk-copy kernel
     (1, 3, 2, 1),  # BF16 on the four-cell kernel
     (1, 2, 0, 7),  # unknown rounding
 ])

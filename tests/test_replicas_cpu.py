@@ -36,7 +36,7 @@ def _rank(rank, world, port, times, out):
 def test_two_gloo_ranks_report_the_slowest_replica():
     world, port = 2, _free_port()
     times = [0.25, 0.40]
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this (threaded) process
         out = m.dict()
         mp.spawn(_rank, args=(world, port, times, out), nprocs=world, join=True)
         res = dict(out)
