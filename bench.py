@@ -467,11 +467,22 @@ def run_closure(args):
         torch.cuda.synchronize()
         out["train_s"] += time.perf_counter() - t0
     out["training_curve"] = curve
+    # correction strength: chosen on a validation seed (neither a training nor an evaluation
+    # seed) by the final velocity error, then used on the evaluation seeds next to strength 1
+    best = 1.0
+    if len(args.strengths) > 1:
+        rows = evaluate(c, setup, args.val_seed, fine_steps=args.steps, check_every=args.steps,
+                        strengths=tuple(args.strengths))
+        last = rows[-1]
+        best = min(args.strengths, key=lambda a: last["err_closure" if a == 1.0 else "err_closure@%g" % a])
+        out["validation"] = {"seed": args.val_seed, "rows": rows, "strength": best}
+    out["strength"] = best
     out["eval"] = {}
     for seed in args.eval_seeds:
-        rows = evaluate(c, setup, seed, fine_steps=args.steps, check_every=args.check_every)
+        rows = evaluate(c, setup, seed, fine_steps=args.steps, check_every=args.check_every,
+                        strengths=tuple(sorted({1.0, best})))
         out["eval"][str(seed)] = rows
-    out["timing"] = time_runs(c, setup, args.eval_seeds[0], fine_steps=args.steps)
+    out["timing"] = time_runs(c, setup, args.eval_seeds[0], fine_steps=args.steps, strength=best)
     print(json.dumps(out), flush=True)
 
 
@@ -585,6 +596,9 @@ def main():
     ap.add_argument("--train-blocks", type=int, default=10)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-seeds", type=int, nargs="*", default=[9001, 9002])
+    ap.add_argument("--strengths", type=float, nargs="*", default=[1.0, 0.5, 0.25, 0.1],
+                    help="closure correction strengths tried on the validation seed")
+    ap.add_argument("--val-seed", type=int, default=7001)
     ap.add_argument("--check-every", type=int, default=2000)
     ap.add_argument("--collision", default="kbc", choices=["bgk", "kbc", "mrt", "regularized"])
     ap.add_argument("--taus", type=float, nargs="*", default=[0.51, 0.6, 0.9])

@@ -71,9 +71,18 @@ class Closure:
         assert p.size == self.nparams
         nat.check(self._lib.lbm_closure_set_params(self._h, nat.ptr(p)))
 
-    def apply(self, sim):
-        """Correct the current populations of FluidSimulator `sim` in place."""
-        nat.check(self._lib.lbm_closure_apply(self._h, sim.handle))
+    def apply(self, sim, strength: float = 1.0):
+        """Correct the current populations of FluidSimulator `sim` in place; `strength` scales
+        the correction (the output scale s_out is divided by it for this call)."""
+        if strength == 1.0:
+            nat.check(self._lib.lbm_closure_apply(self._h, sim.handle))
+            return
+        s_in, s_out = self.s_in, self.s_out
+        self.set_scales(s_in, s_out / strength)
+        try:
+            nat.check(self._lib.lbm_closure_apply(self._h, sim.handle))
+        finally:
+            self.set_scales(s_in, s_out)
 
     def predict(self, sim) -> np.ndarray:
         """The correction the closure would add to `sim`, shape (9, ny, nx)."""
@@ -252,37 +261,44 @@ def coarse_velocity_of(sim_fine, factor):
     return blk(jx) / r, blk(jy) / r
 
 
-def evaluate(closure, setup, seed, fine_steps=20000, check_every=2000):
-    """Run the fine lattice and two coarse lattices (without / with the closure) from the
-    coarse-grained initial state; relative L2 velocity error of each against the
-    coarse-grained fine run at every checkpoint."""
+def _run_name(strength):
+    return "closure" if strength == 1.0 else "closure@%g" % strength
+
+
+def evaluate(closure, setup, seed, fine_steps=20000, check_every=2000, strengths=(1.0,)):
+    """Run the fine lattice and coarse lattices without the closure and with it at each
+    correction strength, all from the coarse-grained initial state; relative L2 velocity error
+    of each against the coarse-grained fine run at every checkpoint (keys err_plain,
+    err_closure for strength 1, err_closure@<strength> otherwise)."""
     fine = setup.fine(seed)
-    plain, corr = setup.coarse(), setup.coarse()
-    coarsen(fine, plain, setup.factor, setup.neq_scale)
-    coarsen(fine, corr, setup.factor, setup.neq_scale)
+    plain = setup.coarse()
+    corr = {a: setup.coarse() for a in strengths}
+    for s in [plain] + list(corr.values()):
+        coarsen(fine, s, setup.factor, setup.neq_scale)
     rows = []
     cs = check_every // setup.factor
     assert cs % setup.k_coarse == 0
     for t in range(check_every, fine_steps + 1, check_every):
         fine.step(check_every)
         plain.step(cs)
-        for _ in range(cs // setup.k_coarse):
-            corr.step(setup.k_coarse)
-            closure.apply(corr)
+        for a, s in corr.items():
+            for _ in range(cs // setup.k_coarse):
+                s.step(setup.k_coarse)
+                closure.apply(s, a)
         gx, gy = coarse_velocity_of(fine, setup.factor)
         norm = np.sqrt(np.sum(gx * gx + gy * gy))
         row = {"fine_step": t, "fine_nonfinite": fine.nonfinite_count(), "ke_fine": float(0.5 * np.mean(gx * gx + gy * gy))}
-        for name, s in (("plain", plain), ("closure", corr)):
+        for name, s in [("plain", plain)] + [(_run_name(a), s) for a, s in corr.items()]:
             _, ux, uy = s.read_macro()
             row["err_" + name] = float(np.sqrt(np.sum((ux - gx) ** 2 + (uy - gy) ** 2)) / norm)
             row["ke_" + name] = float(0.5 * np.mean(ux.astype(np.float64) ** 2 + uy.astype(np.float64) ** 2))
         rows.append(row)
-    for s in (fine, plain, corr):
+    for s in [fine, plain] + list(corr.values()):
         s.close()
     return rows
 
 
-def time_runs(closure, setup, seed, fine_steps=20000):
+def time_runs(closure, setup, seed, fine_steps=20000, strength=1.0):
     """Device time (CUDA events on the lattices' streams, synchronised) of the plain fine
     run, the plain coarse run and the coarse run with the closure, over the same span."""
     import torch
@@ -312,7 +328,7 @@ def time_runs(closure, setup, seed, fine_steps=20000):
     def run_corr():
         for _ in range(nc // setup.k_coarse):
             corr.step(setup.k_coarse)
-            closure.apply(corr)
+            closure.apply(corr, strength)
 
     out["coarse_closure_s"] = timed(run_corr)
     out["speedup_closure"] = out["fine_s"] / out["coarse_closure_s"]

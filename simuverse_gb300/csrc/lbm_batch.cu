@@ -229,6 +229,7 @@ __global__ void k_batch_flags(const BatchDomain* __restrict__ doms, int ndom, co
                     if (s.vx != 0.0f || s.vy != 0.0f) fl |= FL_MOVING;
                 }
             }
+            fl |= plain_bit(fl);
         }
         flags[dm.cell_off + c] = (uint16_t)fl;
     }
