@@ -366,7 +366,10 @@ typedef struct lbm_batch_config {
     int32_t method;           /* LBM_BATCH_* */
     float ms_per_step;        /* filled by lbm_batch_tune */
     int32_t cells_per_thread; /* 1, or 4 (vector accesses); a tile is cells_per_thread * tile_threads_x wide */
-    int32_t reserved[2];
+    int32_t linear;           /* 1: a tile is a run of tile_threads_x * tile_rows consecutive cells of a
+                                 domain's rows (no partly filled tiles at the right edge); needs
+                                 cells_per_thread 1 and domains below 2^24 cells */
+    int32_t reserved[1];
 } lbm_batch_config;
 
 typedef struct lbm_batch lbm_batch;

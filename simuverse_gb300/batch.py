@@ -59,9 +59,11 @@ class BatchSimulator:
         nat.check(self._lib.lbm_batch_get_config(self._h, ctypes.byref(c)))
         inv = {v: k for k, v in nat.BATCH_METHODS.items()}
         return dict(tile_threads_x=c.tile_threads_x, tile_rows=c.tile_rows, blocks_per_sm=c.blocks_per_sm,
-                    method=inv[c.method], ms_per_step=c.ms_per_step, cells_per_thread=c.cells_per_thread)
+                    method=inv[c.method], ms_per_step=c.ms_per_step, cells_per_thread=c.cells_per_thread,
+                    linear=bool(c.linear))
 
-    def configure(self, tile_threads_x=None, tile_rows=None, blocks_per_sm=None, method=None, cells_per_thread=None):
+    def configure(self, tile_threads_x=None, tile_rows=None, blocks_per_sm=None, method=None, cells_per_thread=None,
+                  linear=None):
         c = nat.BatchConfig()
         nat.check(self._lib.lbm_batch_get_config(self._h, ctypes.byref(c)))
         if tile_threads_x is not None:
@@ -74,6 +76,8 @@ class BatchSimulator:
             c.method = nat.BATCH_METHODS[method]
         if cells_per_thread is not None:
             c.cells_per_thread = int(cells_per_thread)
+        if linear is not None:
+            c.linear = 1 if linear else 0
         nat.check(self._lib.lbm_batch_set_config(self._h, ctypes.byref(c)))
 
     def tune(self, trial_steps: int = 20) -> dict:

@@ -7,8 +7,10 @@
 // (planes of domain d at pop_off[d] + j * pitch * ny), flags / info / macro in pooled
 // arrays at cell_off[d].
 //
-// Work.  Domains are cut into tiles of (cells_per_thread * tx) x ty cells; a tile list
-// covers them all (one cell per thread, or four with vector accesses).
+// Work.  Domains are cut into tiles of (cells_per_thread * tx) x ty cells, or (linear tiles)
+// into runs of tx * ty consecutive cells of the padded rows, which leave no partly filled
+// tile at a domain's right edge; a tile list covers them all (one cell per thread, or four
+// with vector accesses).
 // Method 0: one cooperative persistent launch runs every step: blocks take tiles
 // round-robin, then meet at a grid barrier before the next step.  The barrier spins with
 // a time limit: a block that waits longer sets an error word (LBM_ERR_TIMEOUT), every
@@ -41,6 +43,7 @@ struct BatchDomain {
     size_t cell_off;  // cell offset in the flags / info pools (macro: 3 * cell_off)
     int nx, ny, pitch, scene;
     float omega, speed;
+    float inv_pitch;  // 1 / pitch (row of a linear tile's cell)
 };
 
 struct BarrierState {
@@ -96,17 +99,35 @@ __device__ bool grid_barrier(BarrierState* bar, unsigned target, unsigned long l
     return s_ok != 0;
 }
 
-// one tile = (cells_per_thread * blockDim.x) x blockDim.y cells of one domain
+// one tile = (cells_per_thread * blockDim.x) x blockDim.y cells of one domain, or (CPT == 0,
+// linear tiles) blockDim.x * blockDim.y consecutive cells from cell tl.y of the padded rows
 template <int CPT>
 __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms, int4 tl, const float* __restrict__ A0,
                                             float* __restrict__ B0, uint16_t* __restrict__ flags,
                                             lbm_lattice_info* __restrict__ info, float* __restrict__ macro,
                                             bool write_macro) {
     const BatchDomain dm = doms[tl.x];
-    const int y = tl.z + (int)threadIdx.y;
-    if (y >= dm.ny) return;  // warp-uniform: a warp spans one row
     const float* A = A0 + dm.pop_off;
     float* B = B0 + dm.pop_off;
+    if (CPT == 0) {
+        // cells below 2^24 are exact in FP32, and the quotient's error is far below one row;
+        // the two corrections make the row exact
+        const int c = tl.y + (int)(threadIdx.y * blockDim.x + threadIdx.x);
+        int y = (int)(((float)c + 0.5f) * dm.inv_pitch);
+        int x = c - y * dm.pitch;
+        if (x < 0) { --y; x += dm.pitch; }
+        if (x >= dm.pitch) { ++y; x -= dm.pitch; }
+        if (y >= dm.ny || x >= dm.nx) return;  // past the domain's end, or a padding column
+        if (write_macro)
+            phys_cell_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
+                                             dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+        else
+            phys_cell_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
+                                              dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+        return;
+    }
+    const int y = tl.z + (int)threadIdx.y;
+    if (y >= dm.ny) return;  // warp-uniform: a warp spans one row
     if (CPT == 1) {
         const int x = tl.y + (int)threadIdx.x;
         if (x >= dm.nx) return;
@@ -156,7 +177,7 @@ __global__ void __launch_bounds__(256) k_batch_tiles(const BatchDomain* __restri
 }
 
 // method 2: one domain per launch (the single-lattice one-cell kernel's layout)
-__global__ void __launch_bounds__(128, 16) k_batch_domain(BatchDomain dm, const float* A0, float* B0, uint16_t* flags,
+__global__ void __launch_bounds__(128, 12) k_batch_domain(BatchDomain dm, const float* A0, float* B0, uint16_t* flags,
                                                           lbm_lattice_info* info, float* macro, int write_macro) {
     const int x = blockIdx.x * 128 + threadIdx.x;
     const int y = blockIdx.y;
@@ -309,10 +330,14 @@ int build_tiles(lbm_batch* b) {
     std::vector<int4> tiles;
     for (size_t d = 0; d < b->doms.size(); ++d) {
         const lbm::BatchDomain& dm = b->doms[d];
+        if (b->cfg.linear) {
+            const int run = b->cfg.tile_threads_x * b->cfg.tile_rows, n = dm.pitch * dm.ny;
+            for (int c0 = 0; c0 < n; c0 += run) tiles.push_back(make_int4((int)d, c0, 0, 1));
+            continue;
+        }
         for (int y0 = 0; y0 < dm.ny; y0 += th)
             for (int x0 = 0; x0 < dm.pitch; x0 += tw) tiles.push_back(make_int4((int)d, x0, y0, 0));
     }
-    // largest domains first interleaved: keeps the round-robin assignment balanced
     if (b->d_tiles) cudaFree(b->d_tiles);
     b->d_tiles = nullptr;
     B_CK(cudaMalloc((void**)&b->d_tiles, tiles.size() * sizeof(int4)));
@@ -322,10 +347,15 @@ int build_tiles(lbm_batch* b) {
     return LBM_OK;
 }
 
+// the kernels' CPT template argument: 0 = linear tiles, else cells per thread
+int tile_form(const lbm_batch* b) { return b->cfg.linear ? 0 : b->cfg.cells_per_thread; }
+
 int persistent_grid(lbm_batch* b, int* grid) {
     int per_sm = 0;
     const int threads = b->cfg.tile_threads_x * b->cfg.tile_rows;
-    if (b->cfg.cells_per_thread == 1)
+    if (tile_form(b) == 0)
+        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<0>, threads, 0));
+    else if (tile_form(b) == 1)
         B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<1>, threads, 0));
     else
         B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<4>, threads, 0));
@@ -349,7 +379,11 @@ int launch_persistent(lbm_batch* b, int nsteps, int skip_block, int skip_step, c
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    if (b->cfg.cells_per_thread == 1)
+    if (tile_form(b) == 0)
+        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<0>, (const lbm::BatchDomain*)b->d_doms,
+                                (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
+                                b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
+    else if (tile_form(b) == 1)
         B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<1>, (const lbm::BatchDomain*)b->d_doms,
                                 (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
                                 b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
@@ -397,7 +431,10 @@ int run_steps(lbm_batch* b, int nsteps, int method) {
         for (int s = 0; s < nsteps; ++s) {
             const float* A = b->pool[(b->cur + s) & 1];
             float* B = b->pool[(b->cur + s + 1) & 1];
-            if (b->cfg.cells_per_thread == 1)
+            if (tile_form(b) == 0)
+                lbm::k_batch_tiles<0><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
+                    b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
+            else if (tile_form(b) == 1)
                 lbm::k_batch_tiles<1><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
                     b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
             else
@@ -489,6 +526,7 @@ int lbm_batch_create(int32_t n, const lbm_domain_desc* desc, lbm_batch** out) {
         dm.nx = d.nx;
         dm.ny = d.ny;
         dm.pitch = (d.nx + 3) & ~3;
+        dm.inv_pitch = 1.0f / (float)dm.pitch;
         dm.scene = d.scene;
         dm.omega = 1.0f / d.tau;
         dm.speed = d.speed;
@@ -510,6 +548,7 @@ int lbm_batch_create(int32_t n, const lbm_domain_desc* desc, lbm_batch** out) {
     b->cfg.tile_threads_x = 128;
     b->cfg.tile_rows = 2;
     b->cfg.cells_per_thread = 1;
+    b->cfg.linear = 0;
     b->cfg.blocks_per_sm = 0;
     b->cfg.method = LBM_BATCH_PERSISTENT;
     b->cfg.ms_per_step = 0.0f;
@@ -591,8 +630,16 @@ int lbm_batch_set_config(lbm_batch* b, const lbm_batch_config* cfg) {
     if (cfg->blocks_per_sm < 0 || cfg->blocks_per_sm > 32) return bfail(LBM_ERR_ARG, "blocks_per_sm out of range");
     if (cfg->method < LBM_BATCH_PERSISTENT || cfg->method > LBM_BATCH_DOMAIN_LOOP) return bfail(LBM_ERR_ARG, "unknown method");
     if (cfg->cells_per_thread != 1 && cfg->cells_per_thread != 4) return bfail(LBM_ERR_ARG, "cells_per_thread must be 1 or 4");
+    if (cfg->linear != 0 && cfg->linear != 1) return bfail(LBM_ERR_ARG, "linear must be 0 or 1");
+    if (cfg->linear) {
+        if (cfg->cells_per_thread != 1) return bfail(LBM_ERR_ARG, "linear tiles take one cell per thread");
+        for (const lbm::BatchDomain& dm : b->doms)
+            if ((size_t)dm.pitch * dm.ny >= ((size_t)1 << 24))
+                return bfail(LBM_ERR_ARG, "linear tiles need domains below 2^24 cells");
+    }
     B_CK(cudaStreamSynchronize(b->stream));
-    const bool retile = tx != b->cfg.tile_threads_x || ty != b->cfg.tile_rows || cfg->cells_per_thread != b->cfg.cells_per_thread;
+    const bool retile = tx != b->cfg.tile_threads_x || ty != b->cfg.tile_rows ||
+                        cfg->cells_per_thread != b->cfg.cells_per_thread || cfg->linear != b->cfg.linear;
     b->cfg = *cfg;
     if (retile) B_TRY(build_tiles(b));
     free_graph(b);
@@ -643,7 +690,7 @@ int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best_out
         if (best_out) *best_out = it->second;
         return LBM_OK;
     }
-    const int cpts[] = {1, 4};
+    const int cpts[] = {0, 1, 4};  // 0: linear tiles, one cell per thread
     const int txs[] = {32, 64, 128, 256};
     const int tys[] = {1, 2, 4};
     const int bps[] = {0, 2, 4, 6, 8, 12, 16};
@@ -659,7 +706,9 @@ int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best_out
             if (tx * ty > 256) continue;
             for (int bp : bps) {
                 lbm_batch_config c = b->cfg;
-                c.cells_per_thread = cpt;
+                if (cpt == 0 && ty != 1) continue;  // a linear run depends on tx * ty only
+                c.cells_per_thread = cpt == 0 ? 1 : cpt;
+                c.linear = cpt == 0 ? 1 : 0;
                 c.tile_threads_x = tx;
                 c.tile_rows = ty;
                 c.blocks_per_sm = bp;

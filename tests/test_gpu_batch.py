@@ -1,4 +1,4 @@
-"""Batched form: every method agrees with single-lattice runs of the same domains; the
+"""Batched form: every method and tile form agrees with single-lattice runs of the same domains; the
 persistent kernel's bounded grid barrier reports a missing arrival as LBM_ERR_TIMEOUT
 and leaves the context usable; the autotuner returns a working configuration."""
 import numpy as np
@@ -26,11 +26,20 @@ def _single(d, steps):
     return sim
 
 
-@pytest.mark.parametrize("method", ["persistent", "tile_launches", "domain_loop"])
-def test_batch_matches_single_lattices(gpu, method):
+FORMS = {
+    "rows": dict(cells_per_thread=1, linear=False, tile_threads_x=128, tile_rows=2),
+    "linear": dict(cells_per_thread=1, linear=True, tile_threads_x=64, tile_rows=2),
+    "vector4": dict(cells_per_thread=4, linear=False, tile_threads_x=32, tile_rows=4),
+}
+
+
+@pytest.mark.parametrize("method,form", [("persistent", "rows"), ("persistent", "linear"), ("persistent", "vector4"),
+                                         ("tile_launches", "linear"), ("domain_loop", "rows")])
+def test_batch_matches_single_lattices(gpu, method, form):
     steps = 300
     b = BatchSimulator(DOMAINS)
-    b.configure(method=method)
+    b.configure(method=method, **FORMS[form])
+    assert b.config["linear"] == FORMS[form]["linear"]
     b.step(steps - 100)
     b.step(100)
     b.status()
@@ -81,3 +90,9 @@ def test_autotune_returns_a_working_config(gpu):
     b.status()
     cfg2 = b.tune(trial_steps=5)  # cached
     assert cfg2 == cfg
+
+
+def test_linear_tiles_reject_vector_cells(gpu):
+    b = BatchSimulator(DOMAINS)
+    with pytest.raises(nat.LbmError):
+        b.configure(linear=True, cells_per_thread=4)
