@@ -156,11 +156,15 @@ class FluidSimulator:
         return n.value
 
     # ------------------------------------------------------------------ fields
-    def read_macro(self):
-        """(rho, ux, uy) of the last step as (ny, nx) float32 arrays."""
-        rho = np.empty((self.ny, self.nx), np.float32)
-        ux = np.empty_like(rho)
-        uy = np.empty_like(rho)
+    def read_macro(self, out=None):
+        """(rho, ux, uy) of the last step as (ny, nx) float32 arrays; `out` = three C-contiguous
+        float32 arrays of nx * ny values to fill (page-locked ones copy fastest)."""
+        if out is None:
+            out = tuple(np.empty((self.ny, self.nx), np.float32) for _ in range(3))
+        for a in out:
+            if a.dtype != np.float32 or a.size != self.N or not a.flags.c_contiguous:
+                raise ValueError("read_macro needs C-contiguous float32 arrays of nx*ny values")
+        rho, ux, uy = out
         nat.check(self._lib.lbm_read_macro(self._h, nat.ptr(rho), nat.ptr(ux), nat.ptr(uy)))
         return rho, ux, uy
 
