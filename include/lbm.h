@@ -210,6 +210,10 @@ int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* ap
    host array (rows y-28 .. y+27).  lbm_mask_force_stroke: the cells and record that
    D2Q9Node::add_external_force writes; it returns the number of cells written. */
 int lbm_build_mask(const lbm_params* p, lbm_lattice_info* out);
+/* the channel scene's disks (cx, cy, r per disk, FP64, cap disks at most) and their count in
+   *n; physics-mode lattices build their scene mask on the device from this list, so it is all
+   that lbm_create uploads for a channel.  No counterpart in the reference. */
+int lbm_scene_disks(const lbm_params* p, double* out, int32_t cap, int32_t* n);
 int lbm_mask_add_obstacle(int32_t nx, int32_t ny, lbm_lattice_info* info, int32_t x, int32_t y);
 int lbm_mask_force_stroke(int32_t nx, int32_t ny, int32_t pixel_size, lbm_lattice_info* info, float pos_x,
                           float pos_y, float pre_x, float pre_y);

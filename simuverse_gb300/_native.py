@@ -110,6 +110,7 @@ _SIGNATURES = {
     "lbm_touch_move": [_P, _F, _F],
     "lbm_add_external_force": [_P, _F, _F, _F, _F],
     "lbm_build_mask": [ctypes.POINTER(LbmParams), _P],
+    "lbm_scene_disks": [ctypes.POINTER(LbmParams), _P, _I, _P],
     "lbm_mask_add_obstacle": [_I, _I, _P, _I, _I],
     "lbm_mask_force_stroke": [_I, _I, _I, _P, _F, _F, _F, _F],
     "lbm_set_info": [_P, _P],

@@ -110,22 +110,27 @@ double unit53(std::mt19937_64& g) { return (double)(g() >> 11) * (1.0 / 90071992
 // Channel: walls y = 0 and y = ny-1, Zou-He inlet x = 0 with the parabolic profile of a
 // channel whose walls sit half-way between rows, outflow x = nx-1, and non-overlapping
 // disks (radius U[rmin, rmax], gap >= 2 cells) placed by rejection sampling until the
-// solid fraction is reached.  Returns the number of disks.
-int mask_phys_channel(int nx, int ny, float u_max, uint64_t seed, float frac, float rmin, float rmax,
-                      std::vector<lbm_lattice_info>& out) {
-    out.resize((size_t)nx * ny);
-    const double H = (double)(ny - 2);
-    for (int y = 0; y < ny; ++y)
-        for (int x = 0; x < nx; ++x) {
-            lbm_lattice_info r = make_info(LBM_BULK);
-            if (y == 0 || y == ny - 1) r.material = LBM_BOUNDARY;
-            else if (x == 0) {
-                r.material = LBM_INLET;
-                const double s = (double)y - 0.5;
-                r.vx = (float)(4.0 * (double)u_max * s * (H - s) / (H * H));
-            } else if (x == nx - 1) r.material = LBM_OUTLET;
-            out[(size_t)y * nx + x] = r;
+// solid fraction is reached.
+//
+// The cells of disk (cx, cy, r): lattice points of its bounding box inside [1, nx-2] x
+// [1, ny-2] with (x - cx)^2 + (y - cy)^2 <= r^2, evaluated as rounded FP64 products and sum
+// (the device rasteriser k_raster_disks evaluates the same expression).
+template <class F>
+void disk_cells(int nx, int ny, double cx, double cy, double r, F&& visit) {
+    const int x0 = (int)std::floor(cx - r), x1 = (int)std::ceil(cx + r);
+    const int y0 = (int)std::floor(cy - r), y1 = (int)std::ceil(cy + r);
+    for (int y = y0; y <= y1; ++y)
+        for (int x = x0; x <= x1; ++x) {
+            if (x < 1 || x > nx - 2 || y < 1 || y > ny - 2) continue;
+            const double dx = (double)x - cx, dy = (double)y - cy;
+            if (dx * dx + dy * dy <= r * r) visit((size_t)y * nx + x);
         }
+}
+
+// The disk list (cx, cy, r per disk).  Accepted disks keep a gap of 2 cells, so no cell
+// belongs to two disks and every disk cell is a bulk cell of the base pattern: the solid
+// count is the sum of the disks' cell counts.
+std::vector<double> channel_disks(int nx, int ny, uint64_t seed, float frac, float rmin, float rmax) {
     const long target = (long)std::ceil((double)frac * (double)nx * (double)ny);
     const double xlo = nx / 16 > 2 ? (double)(nx / 16) : 2.0;
     const double xhi = (double)(nx - 1) - (nx / 8 > 2 ? (double)(nx / 8) : 2.0);
@@ -147,18 +152,35 @@ int mask_phys_channel(int nx, int ny, float u_max, uint64_t seed, float frac, fl
         }
         if (!ok) continue;
         disks.push_back(cx); disks.push_back(cy); disks.push_back(r);
-        const int x0 = (int)std::floor(cx - r), x1 = (int)std::ceil(cx + r);
-        const int y0 = (int)std::floor(cy - r), y1 = (int)std::ceil(cy + r);
-        for (int y = y0; y <= y1; ++y)
-            for (int x = x0; x <= x1; ++x) {
-                if (x < 1 || x > nx - 2 || y < 1 || y > ny - 2) continue;
-                const double dx = (double)x - cx, dy = (double)y - cy;
-                if (dx * dx + dy * dy <= r * r) {
-                    lbm_lattice_info& c = out[(size_t)y * nx + x];
-                    if (c.material != LBM_OBSTACLE) { c.material = LBM_OBSTACLE; ++solid; }
-                }
-            }
+        disk_cells(nx, ny, cx, cy, r, [&](size_t) { ++solid; });
     }
+    return disks;
+}
+
+// inlet x velocity of row y (FP64 products in source order, rounded once to FP32); the device
+// builder k_build_scene evaluates the same expression
+float channel_inlet_vx(int y, int ny, float u_max) {
+    const double H = (double)(ny - 2);
+    const double s = (double)y - 0.5;
+    return (float)(4.0 * (double)u_max * s * (H - s) / (H * H));
+}
+
+int mask_phys_channel(int nx, int ny, float u_max, uint64_t seed, float frac, float rmin, float rmax,
+                      std::vector<lbm_lattice_info>& out) {
+    out.resize((size_t)nx * ny);
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            lbm_lattice_info r = make_info(LBM_BULK);
+            if (y == 0 || y == ny - 1) r.material = LBM_BOUNDARY;
+            else if (x == 0) {
+                r.material = LBM_INLET;
+                r.vx = channel_inlet_vx(y, ny, u_max);
+            } else if (x == nx - 1) r.material = LBM_OUTLET;
+            out[(size_t)y * nx + x] = r;
+        }
+    const std::vector<double> disks = channel_disks(nx, ny, seed, frac, rmin, rmax);
+    for (size_t k = 0; k < disks.size(); k += 3)
+        disk_cells(nx, ny, disks[k], disks[k + 1], disks[k + 2], [&](size_t c) { out[c].material = LBM_OBSTACLE; });
     return (int)(disks.size() / 3);
 }
 
@@ -175,6 +197,13 @@ void build_scene_mask(const lbm_params& p, std::vector<lbm_lattice_info>& out) {
         case LBM_SCENE_PERIODIC: out.assign((size_t)p.nx * p.ny, make_info(LBM_BULK)); break;
         default: mask_reference(p.nx, p.ny, p.scene, p.lid_speed, p.inlet_speed, out); break;
     }
+}
+
+// Physics-mode scenes are built on the device (no upload of the info records); the host copy
+// is then built from the same parameters when a host-side path first needs it.
+bool device_scene(const lbm_params& p) {
+    return p.mode == LBM_MODE_PHYSICS &&
+           (p.scene == LBM_SCENE_CAVITY || p.scene == LBM_SCENE_CHANNEL || p.scene == LBM_SCENE_PERIODIC);
 }
 
 // d2q9_node.rs:222-241: cells of rows [y-28, y+28) within radius 28 of (x+0.5, y+0.5)
@@ -262,7 +291,41 @@ int use_device(const lbm_handle* h) {
     return LBM_OK;
 }
 
+// the host copy of the info records (built from the parameters on first use when the scene
+// mask was built on the device; until then the device records equal the parameters' mask)
+void ensure_host_info(lbm_handle* h) {
+    if (!h->host_info_lazy) return;
+    build_scene_mask(h->p, h->host_info);
+    h->host_info_lazy = false;
+}
+
+// the physics-mode scene mask built on the device: the host samples the channel's disk list
+// only (a few thousand numbers) and uploads that instead of the records
+int build_scene_on_device(lbm_handle* h) {
+    std::vector<double> disks;
+    if (h->p.scene == LBM_SCENE_CHANNEL)
+        disks = channel_disks(h->nx, h->ny, h->p.seed, h->p.solid_fraction, h->p.disk_rmin, h->p.disk_rmax);
+    double* d_disks = nullptr;
+    const int nd = (int)(disks.size() / 3);
+    if (nd > 0) {
+        LBM_CK(cudaMalloc((void**)&d_disks, disks.size() * sizeof(double)));
+        cudaError_t e = cudaMemcpyAsync(d_disks, disks.data(), disks.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                        h->stream);
+        if (e == cudaSuccess) e = lbm::launch_build_scene(h, d_disks, nd, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaFree(d_disks);
+        if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "scene mask on the device: %s", cudaGetErrorString(e));
+    } else {
+        LBM_CK(lbm::launch_build_scene(h, nullptr, 0, h->stream));
+    }
+    h->launches += nd > 0 ? 2 : 1;
+    h->host_info.clear();
+    h->host_info_lazy = true;
+    return LBM_OK;
+}
+
 int upload_info_rows(lbm_handle* h, int y0, int y1) {
+    ensure_host_info(h);
     const size_t off = (size_t)y0 * h->nx, cnt = (size_t)(y1 - y0) * h->nx;
     LBM_CK(cudaMemcpyAsync(h->d_info + off, h->host_info.data() + off, cnt * sizeof(lbm_lattice_info),
                            cudaMemcpyHostToDevice, h->stream));
@@ -383,8 +446,13 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
         delete h;
         return fail(LBM_ERR_CUDA, "allocation for a %dx%d lattice failed: %s", p.nx, p.ny, cudaGetErrorString(e));
     }
-    build_scene_mask(p, h->host_info);
-    int r = upload_info_rows(h, 0, h->ny);
+    int r = LBM_OK;
+    if (device_scene(p)) {
+        r = build_scene_on_device(h);
+    } else {
+        build_scene_mask(p, h->host_info);
+        r = upload_info_rows(h, 0, h->ny);
+    }
     if (r == LBM_OK) r = rebuild_flags(h);
     if (r == LBM_OK) r = init_state(h);
     if (r == LBM_OK) r = sync(h);
@@ -452,6 +520,7 @@ int lbm_reset(lbm_handle* h) {
     // reference: only the Poiseuille scene rebuilds its mask (d2q9_node.rs:248-255)
     if (h->p.mode == LBM_MODE_PHYSICS || h->p.scene == LBM_SCENE_POISEUILLE) {
         build_scene_mask(h->p, h->host_info);
+        h->host_info_lazy = false;
         LBM_TRY(upload_info_rows(h, 0, h->ny));
     }
     LBM_TRY(rebuild_flags(h));
@@ -481,6 +550,7 @@ int lbm_add_obstacle(lbm_handle* h, int32_t x, int32_t y) {
     if (x < 0 || x >= h->nx || min_y < 0 || max_y > h->ny)
         return fail(LBM_ERR_ARG, "obstacle rows [%d, %d) or column %d outside the lattice", min_y, max_y, x);
     LBM_TRY(use_device(h));
+    ensure_host_info(h);
     obstacle_disc(h->nx, x, y, h->host_info.data());
     // the reference uploads whole rows from its host copy (d2q9_node.rs:243-244)
     LBM_TRY(upload_info_rows(h, min_y, max_y));
@@ -543,6 +613,7 @@ int lbm_add_external_force(lbm_handle* h, float pos_x, float pos_y, float pre_x,
 int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* applied) {
     LBM_TRY(check_handle(h));
     if (n < 0 || (n > 0 && !edits)) return fail(LBM_ERR_ARG, "bad edit list");
+    ensure_host_info(h);
     // resolve the list on the host exactly as the single calls would (guards, touch state,
     // stroke geometry), then let two kernels write the device mask
     float pre_x = h->pre_x, pre_y = h->pre_y;
@@ -666,6 +737,18 @@ int lbm_build_mask(const lbm_params* p, lbm_lattice_info* out) {
     return LBM_OK;
 }
 
+int lbm_scene_disks(const lbm_params* p, double* out, int32_t cap, int32_t* n) {
+    if (!p || !n || cap < 0 || (cap > 0 && !out)) return fail(LBM_ERR_ARG, "bad argument");
+    LBM_TRY(validate_params(*p));
+    *n = 0;
+    if (p->mode != LBM_MODE_PHYSICS || p->scene != LBM_SCENE_CHANNEL) return LBM_OK;
+    const std::vector<double> d = channel_disks(p->nx, p->ny, p->seed, p->solid_fraction, p->disk_rmin, p->disk_rmax);
+    const int32_t nd = (int32_t)(d.size() / 3);
+    if (cap > 0 && nd > 0) std::memcpy(out, d.data(), (size_t)std::min(nd, cap) * 3 * sizeof(double));
+    *n = nd;
+    return LBM_OK;
+}
+
 int lbm_mask_add_obstacle(int32_t nx, int32_t ny, lbm_lattice_info* info, int32_t x, int32_t y) {
     if (!info) return fail(LBM_ERR_ARG, "null info");
     const int r = (int)OBSTACLE_RADIUS;
@@ -690,6 +773,7 @@ int lbm_set_info(lbm_handle* h, const lbm_lattice_info* info) {
     if (!info) return fail(LBM_ERR_ARG, "null info");
     LBM_TRY(use_device(h));
     h->host_info.assign(info, info + h->N);
+    h->host_info_lazy = false;
     LBM_TRY(upload_info_rows(h, 0, h->ny));
     LBM_TRY(rebuild_flags(h));
     return sync(h);
@@ -870,6 +954,7 @@ int lbm_save(lbm_handle* h, const char* path) {
     bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
     ok = ok && std::fwrite(state.data(), 1, state.size(), f) == state.size();
     ok = ok && std::fwrite(info.data(), sizeof(lbm_lattice_info), h->N, f) == h->N;
+    ensure_host_info(h);
     ok = ok && std::fwrite(h->host_info.data(), sizeof(lbm_lattice_info), h->N, f) == h->N;
     ok = ok && std::fwrite(macro.data(), sizeof(float), 3 * h->N, f) == 3 * h->N;
     ok = (std::fclose(f) == 0) && ok;
@@ -912,6 +997,7 @@ int lbm_load(lbm_handle* h, const char* path) {
     LBM_CK(cudaMemcpy(h->d_info, info.data(), h->N * sizeof(lbm_lattice_info), cudaMemcpyHostToDevice));
     LBM_CK(cudaMemcpy(h->d_macro, macro.data(), 3 * h->N * sizeof(float), cudaMemcpyHostToDevice));
     h->host_info = hinfo;
+    h->host_info_lazy = false;
     h->host_mirror_valid = false;
     h->cur = hd.cur & 1;
     h->tau = hd.tau;

@@ -24,6 +24,7 @@ struct lbm_handle {
     uint16_t* d_flags = nullptr;
     lbm_lattice_info* d_info = nullptr;
     std::vector<lbm_lattice_info> host_info;  // D2Q9Node::lattice_info_data
+    bool host_info_lazy = false;  // host_info not built yet: the scene mask was built on the device
     float* d_macro = nullptr;                 // rho, ux, uy planes
     double* d_part = nullptr;                 // reduction partials
     unsigned long long* d_count = nullptr;
@@ -55,6 +56,9 @@ inline size_t dtype_size(int dtype) { return dtype == LBM_DTYPE_F64 ? 8 : (dtype
 
 // Kernel launchers (lbm_kernels.cu).  All return cudaGetLastError() of the launch.
 cudaError_t launch_build_flags(const lbm_handle* h, cudaStream_t s);
+// physics-mode scene mask on the device: base pattern of p's scene, then the disks
+// (cx, cy, r triples in device memory) as obstacles
+cudaError_t launch_build_scene(lbm_handle* h, const double* d_disks, int ndisks, cudaStream_t s);
 cudaError_t launch_ref_init(lbm_handle* h, cudaStream_t s);
 cudaError_t launch_phys_init(lbm_handle* h, const float* d_rho, const float* d_ux, const float* d_uy,
                              cudaStream_t s);

@@ -71,6 +71,61 @@ __global__ void k_build_flags(const lbm_lattice_info* __restrict__ info, uint16_
 }
 
 // ------------------------------------------------------------------------------------
+// physics-mode scene masks on the device.  The expressions are the host builder's
+// (mask_phys_cavity, mask_phys_channel, disk_cells in lbm_api.cpp) with every FP64 product,
+// sum and quotient rounded separately, so the records are bit-identical to the host copy.
+// ------------------------------------------------------------------------------------
+__global__ void k_build_scene(lbm_lattice_info* __restrict__ info, int nx, int ny, int scene, float lid, float u_max) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= nx) return;
+    lbm_lattice_info r;
+    r.material = LBM_BULK;
+    r.block_iter = -1;
+    r.vx = 0.0f;
+    r.vy = 0.0f;
+    if (scene == LBM_SCENE_CAVITY) {
+        if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1) r.material = LBM_BOUNDARY;
+        if (y == 0 && x >= 1 && x <= nx - 2) r.vx = lid;
+    } else if (scene == LBM_SCENE_CHANNEL) {
+        if (y == 0 || y == ny - 1) {
+            r.material = LBM_BOUNDARY;
+        } else if (x == 0) {
+            r.material = LBM_INLET;
+            const double H = (double)(ny - 2), s = (double)y - 0.5;
+            r.vx = (float)__ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(4.0, (double)u_max), s), __dsub_rn(H, s)),
+                                    __dmul_rn(H, H));
+        } else if (x == nx - 1) {
+            r.material = LBM_OUTLET;
+        }
+    }
+    info[(size_t)y * nx + x] = r;
+}
+
+// one block per disk: the lattice points of its bounding box inside [1, nx-2] x [1, ny-2]
+// with (x - cx)^2 + (y - cy)^2 <= r^2 become obstacles
+__global__ void k_raster_disks(lbm_lattice_info* __restrict__ info, int nx, int ny, const double* __restrict__ disks) {
+    const double cx = disks[3 * blockIdx.x], cy = disks[3 * blockIdx.x + 1], r = disks[3 * blockIdx.x + 2];
+    const int x0 = (int)floor(__dsub_rn(cx, r)), x1 = (int)ceil(__dadd_rn(cx, r));
+    const int y0 = (int)floor(__dsub_rn(cy, r)), y1 = (int)ceil(__dadd_rn(cy, r));
+    const int w = x1 - x0 + 1, n = w * (y1 - y0 + 1);
+    const double r2 = __dmul_rn(r, r);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int x = x0 + i % w, y = y0 + i / w;
+        if (x < 1 || x > nx - 2 || y < 1 || y > ny - 2) continue;
+        const double dx = __dsub_rn((double)x, cx), dy = __dsub_rn((double)y, cy);
+        if (__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) <= r2) info[(size_t)y * nx + x].material = LBM_OBSTACLE;
+    }
+}
+
+cudaError_t launch_build_scene(lbm_handle* h, const double* d_disks, int ndisks, cudaStream_t s) {
+    const dim3 grid((unsigned)((h->nx + 255) / 256), (unsigned)h->ny);
+    k_build_scene<<<grid, 256, 0, s>>>(h->d_info, h->nx, h->ny, h->p.scene, h->p.lid_speed, h->p.inlet_speed);
+    if (ndisks > 0) k_raster_disks<<<(unsigned)ndisks, 256, 0, s>>>(h->d_info, h->nx, h->ny, d_disks);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------
 // initialisation
 // ------------------------------------------------------------------------------------
 // init.wgsl:19-63

@@ -27,36 +27,57 @@ import numpy as np
 from . import _native as nat
 
 
+def make_params(nx: int, ny: int, *, mode: str = "reference", dtype: str = "f32", scene: str = "poiseuille",
+                tau: float = None, viscosity: float = None, lid_speed: float = None, inlet_speed: float = None,
+                solid_fraction: float = 0.05, disk_radius=(8.0, 32.0), seed: int = 0, pixel_size: int = 2,
+                macro_every_step: bool = False, kernel: str = "auto", collision: str = "bgk",
+                rounding: str = "nearest") -> "nat.LbmParams":
+    """lbm_params from keyword arguments (lbm_params_default for the rest)."""
+    lib = nat.load()
+    p = nat.LbmParams()
+    lib.lbm_params_default(ctypes.byref(p))
+    p.nx, p.ny = int(nx), int(ny)
+    p.mode = nat.MODES[mode]
+    p.dtype = nat.DTYPES[dtype]
+    p.scene = nat.SCENES[scene]
+    if tau is not None:
+        p.tau = float(tau)
+    elif viscosity is not None:
+        p.tau = float(np.float32(3.0) * np.float32(viscosity) + np.float32(0.5))
+    if lid_speed is not None:
+        p.lid_speed = float(lid_speed)
+    if inlet_speed is not None:
+        p.inlet_speed = float(inlet_speed)
+    p.solid_fraction = float(solid_fraction)
+    p.disk_rmin, p.disk_rmax = float(disk_radius[0]), float(disk_radius[1])
+    p.seed = int(seed)
+    p.pixel_size = int(pixel_size)
+    p.macro_every_step = 1 if macro_every_step else 0
+    p.kernel = nat.KERNELS[kernel]
+    p.collision = nat.COLLISIONS[collision]
+    p.rounding = nat.ROUNDINGS[rounding]
+    return p
+
+
+def scene_disks(nx: int, ny: int, **kw) -> np.ndarray:
+    """The channel scene's disks as an (n, 3) array of (cx, cy, r) (lbm_scene_disks); empty for
+    other scenes."""
+    lib = nat.load()
+    p = make_params(nx, ny, **kw)
+    n = ctypes.c_int32()
+    nat.check(lib.lbm_scene_disks(ctypes.byref(p), None, 0, ctypes.byref(n)))
+    out = np.empty((n.value, 3), np.float64)
+    if n.value:
+        nat.check(lib.lbm_scene_disks(ctypes.byref(p), nat.ptr(out), n.value, ctypes.byref(n)))
+    return out
+
+
 class FluidSimulator:
-    def __init__(self, nx: int, ny: int, *, mode: str = "reference", dtype: str = "f32",
-                 scene: str = "poiseuille", tau: float = None, viscosity: float = None,
-                 lid_speed: float = None, inlet_speed: float = None, solid_fraction: float = 0.05,
-                 disk_radius=(8.0, 32.0), seed: int = 0, pixel_size: int = 2,
-                 macro_every_step: bool = False, kernel: str = "auto", collision: str = "bgk",
-                 rounding: str = "nearest"):
+    def __init__(self, nx: int, ny: int, **kw):
         lib = nat.load()
-        p = nat.LbmParams()
-        lib.lbm_params_default(ctypes.byref(p))
-        p.nx, p.ny = int(nx), int(ny)
-        p.mode = nat.MODES[mode]
-        p.dtype = nat.DTYPES[dtype]
-        p.scene = nat.SCENES[scene]
-        if tau is not None:
-            p.tau = float(tau)
-        elif viscosity is not None:
-            p.tau = float(np.float32(3.0) * np.float32(viscosity) + np.float32(0.5))
-        if lid_speed is not None:
-            p.lid_speed = float(lid_speed)
-        if inlet_speed is not None:
-            p.inlet_speed = float(inlet_speed)
-        p.solid_fraction = float(solid_fraction)
-        p.disk_rmin, p.disk_rmax = float(disk_radius[0]), float(disk_radius[1])
-        p.seed = int(seed)
-        p.pixel_size = int(pixel_size)
-        p.macro_every_step = 1 if macro_every_step else 0
-        p.kernel = nat.KERNELS[kernel]
-        p.collision = nat.COLLISIONS[collision]
-        p.rounding = nat.ROUNDINGS[rounding]
+        p = make_params(nx, ny, **kw)
+        mode, dtype, scene = kw.get("mode", "reference"), kw.get("dtype", "f32"), kw.get("scene", "poiseuille")
+        rounding, pixel_size = kw.get("rounding", "nearest"), kw.get("pixel_size", 2)
         h = ctypes.c_void_p()
         nat.check(lib.lbm_create(ctypes.byref(p), ctypes.byref(h)))
         self._lib = lib

@@ -73,6 +73,34 @@ def test_create_rejects_bad_rounding(native, mode, dtype, kernel, rounding):
     assert "round" in native.lbm_last_error().decode()
 
 
+def test_scene_disks_are_the_channel_obstacles(native):
+    """The disk list lbm_create uploads for a channel: non-overlapping with a 2-cell gap, and
+    its rasterisation is exactly the obstacle set of the host mask."""
+    from simuverse_gb300 import _native as nat
+
+    p = nat.LbmParams()
+    native.lbm_params_default(ctypes.byref(p))
+    p.nx, p.ny, p.mode, p.scene, p.seed = 300, 120, 1, nat.SCENES["channel"], 42
+    p.solid_fraction, p.disk_rmin, p.disk_rmax, p.inlet_speed = 0.06, 4.0, 12.0, 0.05
+    n = ctypes.c_int32()
+    assert native.lbm_scene_disks(ctypes.byref(p), None, 0, ctypes.byref(n)) == 0
+    assert n.value > 5
+    d = np.empty((n.value, 3), np.float64)
+    assert native.lbm_scene_disks(ctypes.byref(p), nat.ptr(d), n.value, ctypes.byref(n)) == 0
+    for i in range(len(d)):
+        for j in range(i):
+            assert np.hypot(d[i, 0] - d[j, 0], d[i, 1] - d[j, 1]) >= d[i, 2] + d[j, 2] + 2.0
+    mask = np.empty((p.ny, p.nx), dtype=nat.INFO_DTYPE)
+    nat.check(native.lbm_build_mask(ctypes.byref(p), nat.ptr(mask)))
+    y, x = np.mgrid[0:p.ny, 0:p.nx].astype(np.float64)
+    inner = (x >= 1) & (x <= p.nx - 2) & (y >= 1) & (y <= p.ny - 2)
+    ras = np.zeros((p.ny, p.nx), bool)
+    for cx, cy, r in d:
+        ras |= inner & ((x - cx) ** 2 + (y - cy) ** 2 <= r * r)
+    assert np.array_equal(ras, mask["material"] == 4)
+    assert ras.sum() >= 0.06 * p.nx * p.ny
+
+
 def test_null_handles_are_errors(native):
     from simuverse_gb300 import _native as nat
 
