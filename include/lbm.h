@@ -373,7 +373,8 @@ typedef struct lbm_batch_config {
     int32_t linear;           /* 1: a tile is a run of tile_threads_x * tile_rows consecutive cells of a
                                  domain's rows (no partly filled tiles at the right edge); needs
                                  cells_per_thread 1 and domains below 2^24 cells */
-    int32_t reserved[1];
+    int32_t full_occupancy;   /* one cell per thread: 1 = kernels compiled for 32 registers (8 blocks of
+                                 256 threads per SM, some spills), 0 = for 40 (6 blocks) */
 } lbm_batch_config;
 
 typedef struct lbm_batch lbm_batch;

@@ -75,7 +75,7 @@ class BatchConfig(ctypes.Structure):
     _fields_ = [("tile_threads_x", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
                 ("blocks_per_sm", ctypes.c_int32), ("method", ctypes.c_int32),
                 ("ms_per_step", ctypes.c_float), ("cells_per_thread", ctypes.c_int32),
-                ("linear", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+                ("linear", ctypes.c_int32), ("full_occupancy", ctypes.c_int32)]
 
 
 BATCH_METHODS = {"persistent": 0, "tile_launches": 1, "domain_loop": 2}

@@ -60,10 +60,10 @@ class BatchSimulator:
         inv = {v: k for k, v in nat.BATCH_METHODS.items()}
         return dict(tile_threads_x=c.tile_threads_x, tile_rows=c.tile_rows, blocks_per_sm=c.blocks_per_sm,
                     method=inv[c.method], ms_per_step=c.ms_per_step, cells_per_thread=c.cells_per_thread,
-                    linear=bool(c.linear))
+                    linear=bool(c.linear), full_occupancy=bool(c.full_occupancy))
 
     def configure(self, tile_threads_x=None, tile_rows=None, blocks_per_sm=None, method=None, cells_per_thread=None,
-                  linear=None):
+                  linear=None, full_occupancy=None):
         c = nat.BatchConfig()
         nat.check(self._lib.lbm_batch_get_config(self._h, ctypes.byref(c)))
         if tile_threads_x is not None:
@@ -78,6 +78,8 @@ class BatchSimulator:
             c.cells_per_thread = int(cells_per_thread)
         if linear is not None:
             c.linear = 1 if linear else 0
+        if full_occupancy is not None:
+            c.full_occupancy = 1 if full_occupancy else 0
         nat.check(self._lib.lbm_batch_set_config(self._h, ctypes.byref(c)))
 
     def tune(self, trial_steps: int = 20) -> dict:

@@ -30,6 +30,7 @@
 #include <random>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "lbm_cell4.cuh"
@@ -149,9 +150,15 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
     }
 }
 
+// Kernel form KF: the tile form (KF % 10: 0 linear tiles, 1 one cell per thread, 4 four cells)
+// and the register budget of the one-cell forms: 40 registers (6 blocks of 256 threads per SM,
+// a few bytes of spills) for KF < 10, 32 registers (8 blocks: full occupancy, more spills) for
+// KF >= 10; the autotuner times both.  Four cells per thread take their natural 128+.
+constexpr int batch_min_blocks(int kf) { return kf >= 10 ? 8 : (kf == 4 ? 1 : 6); }
+
 // method 0: all steps in one cooperative launch
-template <int CPT>
-__global__ void __launch_bounds__(256) k_batch_persistent(const BatchDomain* __restrict__ doms,
+template <int KF>
+__global__ void __launch_bounds__(256, batch_min_blocks(KF)) k_batch_persistent(const BatchDomain* __restrict__ doms,
                                                           const int4* __restrict__ tiles, int ntiles, float* pool0,
                                                           float* pool1, uint16_t* flags, lbm_lattice_info* info,
                                                           float* macro, int nsteps, int cur0, BarrierState* bar,
@@ -162,18 +169,18 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BatchDomain* __r
         float* B = odd ? pool0 : pool1;
         const bool mac = (s == nsteps - 1);
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
-            tile_update<CPT>(doms, tiles[t], A, B, flags, info, macro, mac);
+            tile_update<KF % 10>(doms, tiles[t], A, B, flags, info, macro, mac);
         if ((int)blockIdx.x == skip_block && s == skip_step) return;  // injected missing arrival (tests)
         if (!grid_barrier(bar, (unsigned)(s + 1) * gridDim.x, timeout_ns, s)) return;
     }
 }
 
 // method 1: one step over the tile list, one tile per block
-template <int CPT>
-__global__ void __launch_bounds__(256) k_batch_tiles(const BatchDomain* __restrict__ doms, const int4* __restrict__ tiles,
+template <int KF>
+__global__ void __launch_bounds__(256, batch_min_blocks(KF)) k_batch_tiles(const BatchDomain* __restrict__ doms, const int4* __restrict__ tiles,
                                                      const float* A, float* B, uint16_t* flags, lbm_lattice_info* info,
                                                      float* macro, int write_macro) {
-    tile_update<CPT>(doms, tiles[blockIdx.x], A, B, flags, info, macro, write_macro != 0);
+    tile_update<KF % 10>(doms, tiles[blockIdx.x], A, B, flags, info, macro, write_macro != 0);
 }
 
 // method 2: one domain per launch (the single-lattice one-cell kernel's layout)
@@ -347,18 +354,32 @@ int build_tiles(lbm_batch* b) {
     return LBM_OK;
 }
 
-// the kernels' CPT template argument: 0 = linear tiles, else cells per thread
-int tile_form(const lbm_batch* b) { return b->cfg.linear ? 0 : b->cfg.cells_per_thread; }
+// the kernels' form KF (k_batch_persistent): tile form + 10 for the 32-register budget
+int tile_form(const lbm_batch* b) {
+    const int f = b->cfg.linear ? 0 : b->cfg.cells_per_thread;
+    return f != 4 && b->cfg.full_occupancy ? f + 10 : f;
+}
+
+// calls fn(std::integral_constant<int, KF>) for the configured form
+template <class F>
+int with_form(const lbm_batch* b, F&& fn) {
+    switch (tile_form(b)) {
+        case 0: return fn(std::integral_constant<int, 0>{});
+        case 1: return fn(std::integral_constant<int, 1>{});
+        case 10: return fn(std::integral_constant<int, 10>{});
+        case 11: return fn(std::integral_constant<int, 11>{});
+        default: return fn(std::integral_constant<int, 4>{});
+    }
+}
 
 int persistent_grid(lbm_batch* b, int* grid) {
     int per_sm = 0;
     const int threads = b->cfg.tile_threads_x * b->cfg.tile_rows;
-    if (tile_form(b) == 0)
-        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<0>, threads, 0));
-    else if (tile_form(b) == 1)
-        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<1>, threads, 0));
-    else
-        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<4>, threads, 0));
+    B_TRY(with_form(b, [&](auto kf) {
+        B_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbm::k_batch_persistent<decltype(kf)::value>,
+                                                           threads, 0));
+        return LBM_OK;
+    }));
     if (per_sm < 1) return bfail(LBM_ERR_ARG, "persistent kernel does not fit %d threads per block", threads);
     const int want = b->cfg.blocks_per_sm > 0 ? b->cfg.blocks_per_sm : per_sm;
     *grid = std::min(want, per_sm) * b->sms;
@@ -379,18 +400,12 @@ int launch_persistent(lbm_batch* b, int nsteps, int skip_block, int skip_step, c
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    if (tile_form(b) == 0)
-        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<0>, (const lbm::BatchDomain*)b->d_doms,
+    B_TRY(with_form(b, [&](auto kf) {
+        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<decltype(kf)::value>, (const lbm::BatchDomain*)b->d_doms,
                                 (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
                                 b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
-    else if (tile_form(b) == 1)
-        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<1>, (const lbm::BatchDomain*)b->d_doms,
-                                (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
-                                b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
-    else
-        B_CK(cudaLaunchKernelEx(&lc, lbm::k_batch_persistent<4>, (const lbm::BatchDomain*)b->d_doms,
-                                (const int4*)b->d_tiles, b->ntiles, b->pool[0], b->pool[1], b->d_flags, b->d_info,
-                                b->d_macro, nsteps, b->cur, b->d_bar, b->timeout_ns, skip_block, skip_step));
+        return LBM_OK;
+    }));
     return LBM_OK;
 }
 
@@ -431,15 +446,11 @@ int run_steps(lbm_batch* b, int nsteps, int method) {
         for (int s = 0; s < nsteps; ++s) {
             const float* A = b->pool[(b->cur + s) & 1];
             float* B = b->pool[(b->cur + s + 1) & 1];
-            if (tile_form(b) == 0)
-                lbm::k_batch_tiles<0><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
+            B_TRY(with_form(b, [&](auto kf) {
+                lbm::k_batch_tiles<decltype(kf)::value><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
                     b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
-            else if (tile_form(b) == 1)
-                lbm::k_batch_tiles<1><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
-                    b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
-            else
-                lbm::k_batch_tiles<4><<<(unsigned)b->ntiles, block, 0, b->stream>>>(
-                    b->d_doms, b->d_tiles, A, B, b->d_flags, b->d_info, b->d_macro, s == nsteps - 1);
+                return LBM_OK;
+            }));
             B_CK(cudaGetLastError());
         }
         b->launches += nsteps;
@@ -549,6 +560,7 @@ int lbm_batch_create(int32_t n, const lbm_domain_desc* desc, lbm_batch** out) {
     b->cfg.tile_rows = 2;
     b->cfg.cells_per_thread = 1;
     b->cfg.linear = 0;
+    b->cfg.full_occupancy = 0;
     b->cfg.blocks_per_sm = 0;
     b->cfg.method = LBM_BATCH_PERSISTENT;
     b->cfg.ms_per_step = 0.0f;
@@ -631,6 +643,7 @@ int lbm_batch_set_config(lbm_batch* b, const lbm_batch_config* cfg) {
     if (cfg->method < LBM_BATCH_PERSISTENT || cfg->method > LBM_BATCH_DOMAIN_LOOP) return bfail(LBM_ERR_ARG, "unknown method");
     if (cfg->cells_per_thread != 1 && cfg->cells_per_thread != 4) return bfail(LBM_ERR_ARG, "cells_per_thread must be 1 or 4");
     if (cfg->linear != 0 && cfg->linear != 1) return bfail(LBM_ERR_ARG, "linear must be 0 or 1");
+    if (cfg->full_occupancy != 0 && cfg->full_occupancy != 1) return bfail(LBM_ERR_ARG, "full_occupancy must be 0 or 1");
     if (cfg->linear) {
         if (cfg->cells_per_thread != 1) return bfail(LBM_ERR_ARG, "linear tiles take one cell per thread");
         for (const lbm::BatchDomain& dm : b->doms)
@@ -690,7 +703,7 @@ int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best_out
         if (best_out) *best_out = it->second;
         return LBM_OK;
     }
-    const int cpts[] = {0, 1, 4};  // 0: linear tiles, one cell per thread
+    const int cpts[] = {0, 1, 4, 10, 11};  // 0: linear tiles; + 10: the 32-register budget
     const int txs[] = {32, 64, 128, 256};
     const int tys[] = {1, 2, 4};
     const int bps[] = {0, 2, 4, 6, 8, 12, 16};
@@ -706,9 +719,10 @@ int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best_out
             if (tx * ty > 256) continue;
             for (int bp : bps) {
                 lbm_batch_config c = b->cfg;
-                if (cpt == 0 && ty != 1) continue;  // a linear run depends on tx * ty only
-                c.cells_per_thread = cpt == 0 ? 1 : cpt;
-                c.linear = cpt == 0 ? 1 : 0;
+                if (cpt % 10 == 0 && ty != 1) continue;  // a linear run depends on tx * ty only
+                c.cells_per_thread = cpt % 10 == 0 ? 1 : cpt % 10;
+                c.linear = cpt % 10 == 0 ? 1 : 0;
+                c.full_occupancy = cpt >= 10 ? 1 : 0;
                 c.tile_threads_x = tx;
                 c.tile_rows = ty;
                 c.blocks_per_sm = bp;

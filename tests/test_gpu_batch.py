@@ -27,14 +27,18 @@ def _single(d, steps):
 
 
 FORMS = {
-    "rows": dict(cells_per_thread=1, linear=False, tile_threads_x=128, tile_rows=2),
-    "linear": dict(cells_per_thread=1, linear=True, tile_threads_x=64, tile_rows=2),
-    "vector4": dict(cells_per_thread=4, linear=False, tile_threads_x=32, tile_rows=4),
+    "rows": dict(cells_per_thread=1, linear=False, tile_threads_x=128, tile_rows=2, full_occupancy=False),
+    "rows32": dict(cells_per_thread=1, linear=False, tile_threads_x=64, tile_rows=4, full_occupancy=True),
+    "linear": dict(cells_per_thread=1, linear=True, tile_threads_x=64, tile_rows=2, full_occupancy=False),
+    "linear32": dict(cells_per_thread=1, linear=True, tile_threads_x=256, tile_rows=1, full_occupancy=True),
+    "vector4": dict(cells_per_thread=4, linear=False, tile_threads_x=32, tile_rows=4, full_occupancy=False),
 }
 
 
-@pytest.mark.parametrize("method,form", [("persistent", "rows"), ("persistent", "linear"), ("persistent", "vector4"),
-                                         ("tile_launches", "linear"), ("domain_loop", "rows")])
+@pytest.mark.parametrize("method,form", [("persistent", "rows"), ("persistent", "rows32"), ("persistent", "linear"),
+                                         ("persistent", "linear32"), ("persistent", "vector4"),
+                                         ("tile_launches", "linear"), ("tile_launches", "rows32"),
+                                         ("domain_loop", "rows")])
 def test_batch_matches_single_lattices(gpu, method, form):
     steps = 300
     b = BatchSimulator(DOMAINS)
