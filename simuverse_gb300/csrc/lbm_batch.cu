@@ -108,8 +108,6 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
                                             lbm_lattice_info* __restrict__ info, float* __restrict__ macro,
                                             bool write_macro) {
     const BatchDomain dm = doms[tl.x];
-    const float* A = A0 + dm.pop_off;
-    float* B = B0 + dm.pop_off;
     if (CPT == 0) {
         // cells below 2^24 are exact in FP32, and the quotient's error is far below one row;
         // the two corrections make the row exact
@@ -119,12 +117,13 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
         if (x < 0) { --y; x += dm.pitch; }
         if (x >= dm.pitch) { ++y; x -= dm.pitch; }
         if (y >= dm.ny || x >= dm.nx) return;  // past the domain's end, or a padding column
+        // pool base pointers and the domain's offsets (not per-domain pointers: fewer registers)
         if (write_macro)
-            phys_cell_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
-                                             dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+            phys_cell_update<StoreF32, true, LBM_COLLISION_BGK, false, size_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
         else
-            phys_cell_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
-                                              dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+            phys_cell_update<StoreF32, false, LBM_COLLISION_BGK, false, size_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
         return;
     }
     const int y = tl.z + (int)threadIdx.y;
@@ -133,14 +132,16 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
         const int x = tl.y + (int)threadIdx.x;
         if (x >= dm.nx) return;
         if (write_macro)
-            phys_cell_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
-                                             dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+            phys_cell_update<StoreF32, true, LBM_COLLISION_BGK, false, size_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
         else
-            phys_cell_update<StoreF32, false>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x, y, dm.nx,
-                                              dm.pitch, dm.ny, macro + 3 * dm.cell_off);
+            phys_cell_update<StoreF32, false, LBM_COLLISION_BGK, false, size_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
     } else {
         const int x0 = tl.y + (int)threadIdx.x * 4;
         const bool active = x0 < dm.nx;
+        const float* A = A0 + dm.pop_off;
+        float* B = B0 + dm.pop_off;
         if (write_macro)
             phys_cells4_update<StoreF32, true>(A, B, flags + dm.cell_off, info + dm.cell_off, dm.omega, x0, y, dm.nx,
                                                dm.pitch, dm.ny, active, macro + 3 * dm.cell_off);
@@ -174,7 +175,6 @@ __global__ void __launch_bounds__(256, batch_min_blocks(KF)) k_batch_persistent(
         if (!grid_barrier(bar, (unsigned)(s + 1) * gridDim.x, timeout_ns, s)) return;
     }
 }
-
 // method 1: one step over the tile list, one tile per block
 template <int KF>
 __global__ void __launch_bounds__(256, batch_min_blocks(KF)) k_batch_tiles(const BatchDomain* __restrict__ doms, const int4* __restrict__ tiles,

@@ -281,19 +281,24 @@ __device__ __forceinline__ void bgk_plain_fast(const float (&d)[9], float omega,
 
 // One cell (x, y) of a lattice of nx x ny cells whose rows are `pitch` elements apart
 // (pitch >= nx; the single-lattice kernel passes pitch = nx).
-// SR: stochastic rounding of the stores with the step's `seed` (lbm_common.cuh).
-template <class ST, bool MACRO, int COLL = LBM_COLLISION_BGK, bool SR = false>
+// SR: stochastic rounding of the stores with the step's `seed` (lbm_common.cuh).  A lattice
+// inside a pool (the batched form) passes the pool's base pointers and its element offsets:
+// populations at pop_off, flags and info at cell_off, macro planes at 3 * cell_off; OFF is
+// their integer type (32-bit when the pool allows, which keeps the pointers out of registers).
+template <class ST, bool MACRO, int COLL = LBM_COLLISION_BGK, bool SR = false, class OFF = size_t>
 __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restrict__ A, typename ST::T* __restrict__ B,
                                                  uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                  typename ST::R omega, int x, int y, int nx, int pitch, int ny,
-                                                 float* __restrict__ macro, uint32_t seed = 0) {
+                                                 float* __restrict__ macro, uint32_t seed = 0, OFF pop_off = 0,
+                                                 OFF cell_off = 0) {
     using R = typename ST::R;
-    const size_t N = (size_t)pitch * ny;
+    const OFF N = (OFF)pitch * (OFF)ny;
     const unsigned c = (unsigned)y * (unsigned)pitch + (unsigned)x;  // cells < 2^31
-    const unsigned fl = flags[c];
+    const OFF cc = cell_off + (OFF)c, mc = (OFF)3 * cell_off + (OFF)c;
+    const unsigned fl = flags[cc];
     const int m = (int)(fl & FL_MAT_MASK);
     if (is_solid(m)) {
-        if (MACRO) { macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f; }
+        if (MACRO) { macro[mc] = 0.0f; macro[mc + N] = 0.0f; macro[mc + 2 * N] = 0.0f; }
         return;
     }
     const bool outlet = (m == LBM_OUTLET);
@@ -306,7 +311,7 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
         for (int j = 0; j < 9; ++j) {
             const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
             const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-            d[j] = ST::ldu(A + (size_t)j * N + (row + (unsigned)sx));
+            d[j] = ST::ldu(A + (pop_off + (OFF)j * N + (OFF)(row + (unsigned)sx)));
         }
     } else {
 #pragma unroll
@@ -314,9 +319,9 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
             const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
             const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
             if (fl & (1u << (FL_DIR_SHIFT + j))) {
-                R v = ST::ldu(A + (size_t)INV(j) * N + c);  // half-way bounce-back
+                R v = ST::ldu(A + (pop_off + (OFF)INV(j) * N + (OFF)c));  // half-way bounce-back
                 if (fl & FL_MOVING) {
-                    const lbm_lattice_info si = info[row + sx];
+                    const lbm_lattice_info si = info[cell_off + (OFF)(row + sx)];
                     const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
                     // rounded product, not an FMA: a contracted wall term leaves a
                     // systematic mass drift of ~1e-12 per step in FP32
@@ -324,20 +329,20 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
                 }
                 d[j] = v;
             } else {
-                d[j] = ST::ldu(A + (size_t)j * N + (row + (unsigned)sx));
+                d[j] = ST::ldu(A + (pop_off + (OFF)j * N + (OFF)(row + (unsigned)sx)));
             }
         }
     }
     R o[9], rho, ux, uy;
-    phys_collide<R, COLL>(d, m, fl, c, flags, info, omega, o, rho, ux, uy, R(ST::UNIT));
-    if (MACRO) { macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy; }
+    phys_collide<R, COLL>(d, m, fl, (size_t)cc, flags, info, omega, o, rho, ux, uy, R(ST::UNIT));
+    if (MACRO) { macro[mc] = (float)rho; macro[mc + N] = (float)ux; macro[mc + 2 * N] = (float)uy; }
     if (SR) {
         const uint32_t q = sr_hash(c ^ seed);
 #pragma unroll
-        for (int j = 0; j < 9; ++j) ST::stu_sr(B + (size_t)j * N + c, o[j], q * sr_mul(j));
+        for (int j = 0; j < 9; ++j) ST::stu_sr(B + (pop_off + (OFF)j * N + (OFF)c), o[j], q * sr_mul(j));
     } else {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) ST::stu(B + (size_t)j * N + c, o[j]);
+        for (int j = 0; j < 9; ++j) ST::stu(B + (pop_off + (OFF)j * N + (OFF)c), o[j]);
     }
 }
 
