@@ -145,6 +145,20 @@ def test_apply_conserves_mass_and_momentum(gpu, form):
     assert np.max(np.abs(after[1:] - before[1:])) < 1e-9 * before[0]
 
 
+def test_apply_strength_scales_the_correction(gpu):
+    nx, ny = 128, 64
+    rng = np.random.default_rng(8)
+    c = Closure(nx, ny, seed=8, s_in=20.0, s_out=200.0, inputs="eq", target="populations", projection="cell")
+    c.params = _random_params(c, rng)
+    sim = _turbulent_sim(nx, ny, 6)
+    delta = c.predict(sim).astype(np.float64)
+    f0 = sim.read_populations(np.float64)
+    c.apply(sim, 0.25)
+    got = sim.read_populations(np.float64) - f0
+    assert (c.s_in, c.s_out) == (20.0, 200.0)  # the scale is restored after the call
+    assert np.max(np.abs(got - 0.25 * delta)) <= 1e-6 * np.max(np.abs(delta)) + 1e-9
+
+
 def test_coarsen_conserves_block_sums(gpu):
     F = 4
     fine = _turbulent_sim(256, 128, 6, steps=10)
