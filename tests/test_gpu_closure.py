@@ -156,7 +156,8 @@ def test_apply_strength_scales_the_correction(gpu):
     c.apply(sim, 0.25)
     got = sim.read_populations(np.float64) - f0
     assert (c.s_in, c.s_out) == (20.0, 200.0)  # the scale is restored after the call
-    assert np.max(np.abs(got - 0.25 * delta)) <= 1e-6 * np.max(np.abs(delta)) + 1e-9
+    # FP32: the division by s_out / 0.25 against 0.25 / s_out, and the sum's rounding (|f| < 0.5)
+    assert np.max(np.abs(got - 0.25 * delta)) <= 1e-5 * np.max(np.abs(delta)) + 6e-8
 
 
 def test_coarsen_conserves_block_sums(gpu):
