@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE, NOT PRODUCT CODE.
 
 ctypes wrapper over oracle/lbm_oracle.c, the CPU restatement of simuverse's D2Q9 path.
-Only tests/, ``__graft_entry__.smoke()`` (as the checker) and bench.py's CPU-baseline leg
+Only tests/, ``__graft_entry__.smoke()`` (to check results) and bench.py's CPU-baseline leg
 use it.  Parity status: UNPINNED -- the reference (Rust + WGSL on wgpu) cannot run on
 these machines and its own tests hold no vectors for this path; see lbm_oracle.h.
 """

@@ -2,7 +2,7 @@
  * lbm_oracle.h -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
  *
  * CPU restatement of simuverse's D2Q9 lattice-Boltzmann step, used only by tests/,
- * by __graft_entry__.smoke() as a checker, and by bench.py's CPU-baseline leg.
+ * by __graft_entry__.smoke() to check results, and by bench.py's CPU-baseline leg.
  * The CUDA library (simuverse_gb300/csrc) never links or calls it.
  *
  * Parity status: UNPINNED. The reference is Rust + WGSL executed through wgpu; no Rust
