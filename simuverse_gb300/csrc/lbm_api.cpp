@@ -518,7 +518,10 @@ int lbm_reset(lbm_handle* h) {
     LBM_TRY(check_handle(h));
     LBM_TRY(use_device(h));
     // reference: only the Poiseuille scene rebuilds its mask (d2q9_node.rs:248-255)
-    if (h->p.mode == LBM_MODE_PHYSICS || h->p.scene == LBM_SCENE_POISEUILLE) {
+    if (device_scene(h->p)) {
+        LBM_TRY(build_scene_on_device(h));  // the host copy follows lazily, as after create
+        h->host_mirror_valid = false;       // the device copy of the host copy is stale
+    } else if (h->p.mode == LBM_MODE_PHYSICS || h->p.scene == LBM_SCENE_POISEUILLE) {
         build_scene_mask(h->p, h->host_info);
         h->host_info_lazy = false;
         LBM_TRY(upload_info_rows(h, 0, h->ny));

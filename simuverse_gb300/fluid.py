@@ -74,6 +74,11 @@ def scene_disks(nx: int, ny: int, **kw) -> np.ndarray:
 
 class FluidSimulator:
     def __init__(self, nx: int, ny: int, **kw):
+        """An nx x ny lattice (lbm_create).  Keywords, all optional (make_params): mode
+        ("reference" | "physics"), dtype ("f32" | "f64" | "f16" | "bf16"), scene ("poiseuille" |
+        "cavity" | "custom" | "channel" | "periodic"), tau or viscosity, lid_speed, inlet_speed,
+        solid_fraction, disk_radius, seed, pixel_size, macro_every_step, kernel, collision,
+        rounding ("nearest" | "stochastic")."""
         lib = nat.load()
         p = make_params(nx, ny, **kw)
         mode, dtype, scene = kw.get("mode", "reference"), kw.get("dtype", "f32"), kw.get("scene", "poiseuille")

@@ -79,3 +79,20 @@ def test_checkpoint_and_reset_after_device_scene(gpu, tmp_path):
     assert np.array_equal(b.info().view(np.uint8), _host_mask(nx, ny, **kw).view(np.uint8))
     a.close()
     b.close()
+
+
+def test_edits_after_reset_on_a_device_scene(gpu):
+    """A reset rebuilds the scene on the device; the batched edits that follow start from the
+    initial mask again (their device copy of the host mask is refreshed)."""
+    nx, ny = 256, 128
+    kw = _kw("channel", 13, 0.05, (4.0, 9.0))
+    sim = FluidSimulator(nx, ny, **kw)
+    sim.apply_edits([("obstacle", 60, 64)])
+    sim.step(5)
+    sim.reset()
+    assert np.array_equal(sim.info().view(np.uint8), _host_mask(nx, ny, **kw).view(np.uint8))
+    sim.apply_edits([("obstacle", 180, 64)])
+    expect = _host_mask(nx, ny, **kw)
+    nat.check(nat.load().lbm_mask_add_obstacle(nx, ny, nat.ptr(expect), 180, 64))
+    assert np.array_equal(sim.info().view(np.uint8), expect.view(np.uint8))
+    sim.close()
