@@ -184,3 +184,19 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(nat, "LIB_PATH", str(tmp_path / "absent.so"))
     with pytest.raises(RuntimeError):
         nat.load()
+
+
+def test_python_params_and_scene_disks():
+    from simuverse_gb300.fluid import make_params, scene_disks
+
+    p = make_params(300, 120, mode="physics", dtype="f16", scene="channel", tau=0.7, inlet_speed=0.05, seed=42,
+                    solid_fraction=0.06, disk_radius=(4.0, 12.0), kernel="tiled", rounding="stochastic")
+    assert (p.nx, p.ny, p.mode, p.dtype, p.scene, p.kernel, p.rounding) == (300, 120, 1, 2, 3, 5, 1)
+    assert p.tau == pytest.approx(0.7) and p.seed == 42
+    d = scene_disks(300, 120, mode="physics", scene="channel", inlet_speed=0.05, seed=42, solid_fraction=0.06,
+                    disk_radius=(4.0, 12.0))
+    assert d.shape[1] == 3 and len(d) > 5
+    assert np.all((d[:, 2] >= 4.0) & (d[:, 2] <= 12.0))
+    assert len(scene_disks(64, 64, mode="physics", scene="cavity")) == 0
+    with pytest.raises(KeyError):
+        make_params(64, 64, rounding="sometimes")
