@@ -200,3 +200,20 @@ def test_python_params_and_scene_disks():
     assert len(scene_disks(64, 64, mode="physics", scene="cavity")) == 0
     with pytest.raises(KeyError):
         make_params(64, 64, rounding="sometimes")
+
+
+def test_no_gpu_fails_loudly():
+    """Without a usable GPU every entry point that needs one returns an error (no CPU fallback)."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from simuverse_gb300 import BatchSimulator, FluidSimulator, generate_domains
+    from simuverse_gb300 import _native as nat
+    from simuverse_gb300.closure import Closure
+
+    with pytest.raises(nat.LbmError):
+        FluidSimulator(64, 64, mode="physics", scene="channel")
+    with pytest.raises(nat.LbmError):
+        BatchSimulator(generate_domains(4, 1))
+    with pytest.raises(nat.LbmError):
+        Closure(64, 64)
