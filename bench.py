@@ -131,15 +131,29 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per launch of the step kernel from the committed ncu summary, if any."""
+def effective_kernel(args):
+    """The step kernel LBM_KERNEL_AUTO runs for this configuration."""
+    if args.kernel != "auto":
+        return args.kernel
+    if args.dtype in ("f32", "f64"):
+        return "cell"
+    return "tiled" if args.nx % 64 == 0 else "vec2"
+
+
+def committed_traffic(args):
+    """DRAM bytes per launch of the step kernel from a committed ncu summary of this exact
+    configuration (dtype, size, kernel, rounding), or None."""
     path = os.path.join(ROOT, "profiles", "channel_step_traffic.json")
     try:
         with open(path) as f:
-            d = json.load(f)
-        return d
-    except (OSError, ValueError):
+            entries = json.load(f)["entries"]
+    except (OSError, ValueError, KeyError):
         return None
+    key = (args.dtype, args.nx, args.ny, effective_kernel(args), args.rounding)
+    for e in entries:
+        if (e["dtype"], e["nx"], e["ny"], e["kernel"], e["rounding"]) == key:
+            return e
+    return None
 
 
 def cpu_baseline_sample(args, seconds_cap=15.0):
@@ -244,7 +258,7 @@ def run_gpu(args):
     bytes_per_cell = 18 * BYTES_PER_VALUE[args.dtype]
     achieved = bytes_per_cell * cells / per_launch_s / 1e9
     peak, peak_kind = measured_peak()
-    tr = committed_traffic()
+    tr = committed_traffic(args)
 
     # ---- macro every step (the reference's behaviour), reported separately
     sim_m = FluidSimulator(macro_every_step=True, **params)
