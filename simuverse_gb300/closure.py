@@ -298,6 +298,55 @@ def evaluate(closure, setup, seed, fine_steps=20000, check_every=2000, strengths
     return rows
 
 
+def _kinetic_energy(sim):
+    _, ux, uy = sim.read_macro()
+    return float(0.5 * np.mean(ux.astype(np.float64) ** 2 + uy.astype(np.float64) ** 2))
+
+
+def advance(closure, setup, seed, fine_steps=20000, check_every=2000, strength=1.0, energy_tol=0.02):
+    """Advance the decaying-turbulence case `seed` by fine_steps fine-equivalent steps on the
+    coarse lattice corrected by the closure, with the plain fine lattice as the fallback.
+
+    Every check_every fine-equivalent steps the coarse state must be finite and its kinetic
+    energy must not have grown by more than energy_tol (relative) since the previous check:
+    decaying turbulence only loses energy, so growth marks a correction that feeds the flow.  On a
+    failed check the coarse run is abandoned and the fine lattice, kept at the initial state, runs
+    the whole span instead.  Returns a dict: ux, uy (on the coarse grid: the corrected run's macro
+    field, or the block-averaged fine velocity after a fallback), fallback (bool), failed_at (the
+    fine-equivalent step of the failed check or None), energies (kinetic energy at each check)."""
+    fine = setup.fine(seed)
+    coarse = setup.coarse()
+    coarsen(fine, coarse, setup.factor, setup.neq_scale)
+    cs = check_every // setup.factor
+    assert cs % setup.k_coarse == 0 and fine_steps % check_every == 0
+    energies, failed_at = [], None
+    ke_prev = None
+    for t in range(check_every, fine_steps + 1, check_every):
+        for _ in range(cs // setup.k_coarse):
+            coarse.step(setup.k_coarse)
+            closure.apply(coarse, strength)
+        ke = _kinetic_energy(coarse)
+        energies.append(ke)
+        bad = coarse.nonfinite_count() > 0 or not np.isfinite(ke)
+        if not bad and ke_prev is not None and ke > ke_prev * (1.0 + energy_tol):
+            bad = True
+        if bad:
+            failed_at = t
+            break
+        ke_prev = ke
+    if failed_at is None:
+        _, ux, uy = coarse.read_macro()
+        out = dict(ux=ux, uy=uy, fallback=False)
+    else:
+        fine.step(fine_steps)
+        gx, gy = coarse_velocity_of(fine, setup.factor)
+        out = dict(ux=gx.astype(np.float32), uy=gy.astype(np.float32), fallback=True)
+    out.update(failed_at=failed_at, energies=energies)
+    fine.close()
+    coarse.close()
+    return out
+
+
 def time_runs(closure, setup, seed, fine_steps=20000, strength=1.0):
     """Device time (CUDA events on the lattices' streams, synchronised) of the plain fine
     run, the plain coarse run and the coarse run with the closure, over the same span."""

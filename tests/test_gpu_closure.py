@@ -6,7 +6,7 @@ import pytest
 
 from oracle import closure_ref as ref
 from simuverse_gb300 import FluidSimulator
-from simuverse_gb300.closure import Closure, coarsen
+from simuverse_gb300.closure import Closure, TurbulenceSetup, advance, coarse_velocity_of, coarsen
 from simuverse_gb300.turbulence import random_velocity
 
 pytestmark = pytest.mark.gpu
@@ -226,3 +226,27 @@ def test_closure_gain_over_plain_coarse_run_is_measured(gpu):
     assert np.isfinite(last["err_closure"]) and last["fine_nonfinite"] == 0
     assert last["err_closure"] < 1.5 * last["err_plain"] + 1e-3
     c.close()
+
+
+def test_fine_lattice_is_the_fallback(gpu):
+    """advance(): with a zero correction the closure run is the plain coarse run and passes its
+    checks; a check that always fails hands the span over to the fine lattice."""
+    setup = TurbulenceSetup(nf=256, factor=4, tau_f=0.52, k_coarse=4, collision="kbc")
+    c = Closure(setup.nc, setup.nc, seed=0, inputs="eq", target="populations", projection="cell")
+    c.params = np.zeros_like(c.params)
+    ok = advance(c, setup, 5, fine_steps=512, check_every=128)
+    assert not ok["fallback"] and ok["failed_at"] is None and len(ok["energies"]) == 4
+    fine = setup.fine(5)
+    plain = setup.coarse()
+    coarsen(fine, plain, setup.factor, setup.neq_scale)
+    plain.step(512 // setup.factor)
+    _, ux, uy = plain.read_macro()
+    assert np.array_equal(ok["ux"], ux) and np.array_equal(ok["uy"], uy)
+    fb = advance(c, setup, 5, fine_steps=512, check_every=128, energy_tol=-1.0)
+    assert fb["fallback"] and fb["failed_at"] == 256
+    fine.step(512)
+    gx, gy = coarse_velocity_of(fine, setup.factor)
+    assert np.allclose(fb["ux"], gx, rtol=0, atol=1e-7) and np.allclose(fb["uy"], gy, rtol=0, atol=1e-7)
+    for s_ in (fine, plain):
+        s_.close()
+
