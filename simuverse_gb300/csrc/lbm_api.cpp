@@ -412,6 +412,7 @@ void lbm_params_default(lbm_params* p) {
 }
 
 int lbm_create(const lbm_params* pin, lbm_handle** out) {
+    LbmRange range_("lbm_create");
     if (!pin || !out) return fail(LBM_ERR_ARG, "null argument");
     *out = nullptr;
     const lbm_params& p = *pin;
@@ -498,6 +499,7 @@ int lbm_get_params(const lbm_handle* h, lbm_params* out) {
 }
 
 int lbm_step(lbm_handle* h, int32_t nsteps) {
+    LbmRange range_("lbm_step");
     LBM_TRY(check_handle(h));
     if (nsteps < 0) return fail(LBM_ERR_ARG, "negative step count");
     LBM_TRY(use_device(h));
@@ -515,6 +517,7 @@ int lbm_step(lbm_handle* h, int32_t nsteps) {
 int lbm_compute(lbm_handle* h) { return lbm_step(h, 2); }
 
 int lbm_reset(lbm_handle* h) {
+    LbmRange range_("lbm_reset");
     LBM_TRY(check_handle(h));
     LBM_TRY(use_device(h));
     // reference: only the Poiseuille scene rebuilds its mask (d2q9_node.rs:248-255)
@@ -614,6 +617,7 @@ int lbm_add_external_force(lbm_handle* h, float pos_x, float pos_y, float pre_x,
 }
 
 int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* applied) {
+    LbmRange range_("lbm_apply_edits");
     LBM_TRY(check_handle(h));
     if (n < 0 || (n > 0 && !edits)) return fail(LBM_ERR_ARG, "bad edit list");
     ensure_host_info(h);
@@ -791,6 +795,7 @@ int lbm_get_info(lbm_handle* h, lbm_lattice_info* out) {
 }
 
 int lbm_read_macro(lbm_handle* h, float* rho, float* ux, float* uy) {
+    LbmRange range_("lbm_read_macro");
     LBM_TRY(check_handle(h));
     LBM_TRY(use_device(h));
     float* dst[3] = {rho, ux, uy};
@@ -879,6 +884,7 @@ int lbm_init_equilibrium(lbm_handle* h, const float* rho, const float* ux, const
 }
 
 int lbm_conservation(lbm_handle* h, double out[3]) {
+    LbmRange range_("lbm_conservation");
     LBM_TRY(check_handle(h));
     if (!out) return fail(LBM_ERR_ARG, "null output");
     LBM_TRY(use_device(h));

@@ -667,6 +667,7 @@ int lbm_batch_get_config(const lbm_batch* b, lbm_batch_config* cfg) {
 }
 
 int lbm_batch_step(lbm_batch* b, int32_t nsteps) {
+    LbmRange range_("lbm_batch_step");
     B_TRY(check_batch(b));
     if (nsteps < 0) return bfail(LBM_ERR_ARG, "negative step count");
     B_CK(cudaSetDevice(b->device));
@@ -693,6 +694,7 @@ int lbm_batch_inject_missing_arrival(lbm_batch* b, int32_t nsteps, int32_t block
 }
 
 int lbm_batch_tune(lbm_batch* b, int32_t trial_steps, lbm_batch_config* best_out) {
+    LbmRange range_("lbm_batch_tune");
     B_TRY(check_batch(b));
     if (trial_steps < 1) return bfail(LBM_ERR_ARG, "trial_steps must be >= 1");
     B_CK(cudaSetDevice(b->device));

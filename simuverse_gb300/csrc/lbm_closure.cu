@@ -667,6 +667,7 @@ int lbm_closure_set_params(lbm_closure* c, const float* in) {
 }
 
 int lbm_coarsen(lbm_handle* fine, lbm_handle* coarse, int32_t factor, float neq_scale) {
+    LbmRange range_("lbm_coarsen");
     if (!fine || !coarse) return cfail(LBM_ERR_ARG, "null handle");
     C_TRY(check_coarse(nullptr, fine));
     C_TRY(check_coarse(nullptr, coarse));
@@ -725,6 +726,7 @@ int correction(lbm_closure* c, lbm_handle* h, float* out, int accumulate) {
 extern "C" {
 
 int lbm_closure_apply(lbm_closure* c, lbm_handle* h) {
+    LbmRange range_("lbm_closure_apply");
     C_TRY(check_closure(c));
     C_TRY(check_coarse(c, h));
     C_CK(cudaSetDevice(c->device));
@@ -765,6 +767,7 @@ int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t
 }
 
 int lbm_closure_add_pair(lbm_closure* c, lbm_handle* pred, lbm_handle* target, int32_t ox, int32_t oy) {
+    LbmRange range_("lbm_closure_add_pair");
     C_TRY(check_closure(c));
     C_TRY(check_coarse(nullptr, pred));
     C_TRY(check_coarse(nullptr, target));
@@ -798,6 +801,7 @@ int lbm_closure_pairs(const lbm_closure* c, int32_t* n) {
 // Adam on random batches of stored pairs; loss_out (may be NULL) receives the mean loss of
 // the last iteration
 int lbm_closure_train(lbm_closure* c, int32_t iters, float lr, uint64_t seed, double* loss_out) {
+    LbmRange range_("lbm_closure_train");
     C_TRY(check_closure(c));
     if (c->npairs < 1) return cfail(LBM_ERR_STATE, "no training pairs");
     if (iters < 0 || !(lr > 0.0f)) return cfail(LBM_ERR_ARG, "bad iteration count or learning rate");
@@ -892,6 +896,7 @@ int lbm_closure_loss_grad(lbm_closure* c, int32_t nimg, int32_t size, const floa
 // the correction delta (9 planes of nx * ny floats) the closure would add to the whole
 // lattice h, without applying it (inspection and tests)
 int lbm_closure_predict(lbm_closure* c, lbm_handle* h, float* delta_out) {
+    LbmRange range_("lbm_closure_predict");
     C_TRY(check_closure(c));
     C_TRY(check_coarse(c, h));
     if (!delta_out) return cfail(LBM_ERR_ARG, "null output");

@@ -11,6 +11,22 @@
 
 #include "../../include/lbm.h"
 
+// NVTX ranges around the entry points, visible in Nsight tools (header-only NVTX 3; no ranges
+// where the toolkit lacks it).  One object per call: LbmRange r("lbm_step");
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+struct LbmRange {
+    explicit LbmRange(const char* name) { nvtxRangePushA(name); }
+    ~LbmRange() { nvtxRangePop(); }
+    LbmRange(const LbmRange&) = delete;
+    LbmRange& operator=(const LbmRange&) = delete;
+};
+#else
+struct LbmRange {
+    explicit LbmRange(const char*) {}
+};
+#endif
+
 struct lbm_handle {
     lbm_params p;
     int nx = 0, ny = 0;

@@ -485,6 +485,7 @@ int lbm_particles_info(const lbm_particles* ps, int32_t* num_x, int32_t* num_y) 
 }
 
 int lbm_particles_update(lbm_particles* ps, lbm_handle* h) {
+    LbmRange range_("lbm_particles_update");
     int r = check_pair(ps, h);
     if (r < 0) return r;
     V_CK(cudaSetDevice(ps->device));
@@ -519,6 +520,7 @@ int lbm_particles_update(lbm_particles* ps, lbm_handle* h) {
 }
 
 int lbm_particles_present(lbm_particles* ps, lbm_handle* h, float** d_rgba) {
+    LbmRange range_("lbm_particles_present");
     int r = check_pair(ps, h);
     if (r < 0) return r;
     V_CK(cudaSetDevice(ps->device));
@@ -580,6 +582,7 @@ int lbm_particles_counters(const lbm_particles* ps, uint64_t* updates, uint64_t*
 }
 
 int lbm_curl(lbm_handle* h, float* d_out) {
+    LbmRange range_("lbm_curl");
     if (!h || !d_out) return vfail(LBM_ERR_ARG, "null argument");
     V_CK(cudaSetDevice(h->device));
     if (h->nx % 4 == 0 && ((uintptr_t)d_out & 15) == 0) {
@@ -595,6 +598,7 @@ int lbm_curl(lbm_handle* h, float* d_out) {
 }
 
 int lbm_colorize(lbm_handle* h, int32_t mode, const float* d_curl, int32_t canvas_w, int32_t canvas_h, float* d_rgba) {
+    LbmRange range_("lbm_colorize");
     if (!h || !d_rgba) return vfail(LBM_ERR_ARG, "null argument");
     if (mode != LBM_COLOR_CURL && mode != LBM_COLOR_ANGLE) return vfail(LBM_ERR_ARG, "unknown colour mode %d", mode);
     if (canvas_w < 1 || canvas_h < 1 || canvas_h > 65535) return vfail(LBM_ERR_ARG, "canvas size out of range");
