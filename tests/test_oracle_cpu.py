@@ -69,6 +69,41 @@ def test_rest_state_is_invariant():
     assert np.max(np.abs(p.deviations)) < 1e-15
 
 
+def _periodic_info(nx, ny):
+    info = np.zeros((ny, nx), oracle.INFO_DTYPE)
+    info["material"] = 1
+    info["block_iter"] = -1
+    return info
+
+
+@pytest.mark.parametrize("collision", [0, 1, 2, 3], ids=["bgk", "regularized", "mrt", "kbc"])
+def test_collisions_conserve_mass_and_momentum(collision):
+    """Every collision operator of the oracle conserves mass and momentum (FP64, periodic
+    lattice, a random non-equilibrium state)."""
+    nx, ny = 48, 32
+    p = oracle.PhysOracle(_periodic_info(nx, ny), 0.53, np.float64, collision=collision)
+    rng = np.random.default_rng(collision)
+    p.bufs[p.cur][...] = oracle.PhysOracle.W.reshape(9, 1, 1) * 0.05 * rng.standard_normal((9, ny, nx))
+    before = np.array(p.conservation())
+    p.step(20)
+    after = np.array(p.conservation())
+    assert np.all(np.isfinite(p.deviations))
+    assert abs(after[0] - before[0]) <= 1e-12 * abs(before[0])
+    assert np.max(np.abs(after[1:] - before[1:])) <= 1e-12 * abs(before[0])
+
+
+@pytest.mark.parametrize("collision", [0, 1, 2, 3], ids=["bgk", "regularized", "mrt", "kbc"])
+def test_uniform_flow_equilibrium_is_a_fixed_point(collision):
+    nx, ny = 32, 16
+    p = oracle.PhysOracle(_periodic_info(nx, ny), 0.6, np.float64, collision=collision)
+    ux = np.full((ny, nx), 0.05)
+    uy = np.full((ny, nx), -0.02)
+    p.init_equilibrium(np.full((ny, nx), 1.01), ux, uy)
+    f0 = p.populations().copy()
+    p.step(10)
+    assert np.max(np.abs(p.populations() - f0)) < 1e-13
+
+
 def test_shear_wave_decay_rate():
     nx, ny, tau, U, steps = 32, 128, 0.8, 0.01, 2000
     p = oracle.PhysOracle(oracle.mask_periodic(nx, ny), tau, np.float64)
