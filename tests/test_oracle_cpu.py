@@ -104,6 +104,19 @@ def test_uniform_flow_equilibrium_is_a_fixed_point(collision):
     assert np.max(np.abs(p.populations() - f0)) < 1e-13
 
 
+def test_inlet_velocity_and_outlet_density_are_imposed():
+    """The Zou-He inlet's cells carry exactly the prescribed parabolic velocity, and the anchored
+    outflow keeps the outlet density at 1 (FP64)."""
+    info, _ = oracle.mask_physics_channel(96, 34, 0.05, 1, 0.0, 4.0, 8.0)
+    p = oracle.PhysOracle(info, 0.7, np.float64)
+    p.step(300)
+    rho, ux, uy = p.macro()
+    inlet, outlet = info["material"] == 3, info["material"] == 5
+    assert np.max(np.abs(ux[inlet] - info["vx"][inlet])) < 1e-15
+    assert np.max(np.abs(uy[inlet])) < 1e-15
+    assert np.max(np.abs(rho[outlet] - 1.0)) < 1e-14
+
+
 def test_shear_wave_decay_rate():
     nx, ny, tau, U, steps = 32, 128, 0.8, 0.01, 2000
     p = oracle.PhysOracle(oracle.mask_periodic(nx, ny), tau, np.float64)
