@@ -6,16 +6,23 @@ non-overlapping disks (radius U[8, 32], 5 % solid), tau = 0.56, equilibrium star
 bench step is one LBM time step over the whole lattice.  The working set (2 x 604 MB of
 populations) is larger than L2, so no flush is needed between steps.
 
-Output: one JSON line.  value = cell updates / s / 1e9 over the timed steps (device time,
-CUDA events on the library's stream); e2e = the same metric for the whole job through the
-public API (create from host parameters, mask built and uploaded from the host, K steps,
-macro field read back to host memory); roofline = 72 algorithmic bytes per cell update
-over the measured HBM copy bandwidth; cpu_baseline = the oracle (the CPU restatement of
-the reference path) on the host cores for a bounded sample.
+Output: one JSON line.  value = cell updates / s / 1e9 of K steps (device time, CUDA events
+on the library's stream), the median over `repeats` back-to-back intervals of exactly K
+steps (repeated until about --min-seconds of device time, so that the clock samples see the
+load; `spread` gives the slowest and fastest interval); e2e = the same metric for the whole
+job through the public API (create from host parameters, scene mask built on the device
+from the uploaded disk list, K steps, macro field read back to page-locked host memory);
+roofline = 72 algorithmic bytes per cell update over the measured HBM copy bandwidth;
+cpu_baseline = the oracle (the CPU restatement of the reference path) on the host cores,
+full workload, about 15 s of steps.  `reference_mode_glups` / `reference_mode_exact_glups`:
+the reference's own rules (its Poiseuille scene) at the same size, in the fast and the exact
+arithmetic.  `extras`: the precision form's 8192^2 lattice in FP32, the reference's rules,
+FP16 / BF16 storage, and the batched form (256 seeded domains), each with its roofline
+fraction.
 
---impl reference times that CPU restatement alone (all host threads), the reference
-having no CPU implementation of its own (its path is WGSL run by wgpu, which needs a
-graphics API these machines do not have).
+--impl reference times that CPU restatement alone (all host threads) on the full workload,
+the reference having no CPU implementation of its own (its path is WGSL run by wgpu, which
+needs a graphics API these machines do not have).
 
 Multi-GPU: replicas only -- each rank advances its own copy of the workload; no
 collectives touch the data path.
@@ -157,13 +164,13 @@ def committed_traffic(args):
 
 
 def cpu_baseline_sample(args, seconds_cap=15.0):
-    """The oracle's FP32 physics step on a 4096-wide slice of the channel, all host threads."""
+    """The oracle's FP32 physics step on the full channel workload (all host threads), as
+    many steps as fit in seconds_cap after two warm-up steps."""
     import numpy as np
 
     import oracle
 
-    ny = max(64, min(args.ny, int(os.environ.get("LBM_CPU_SAMPLE_ROWS", "512"))))
-    info, _ = oracle.mask_physics_channel(args.nx, ny, 0.05, 1234, 0.05, 8.0, 32.0)
+    info, _ = oracle.mask_physics_channel(args.nx, args.ny, 0.05, 1234, 0.05, 8.0, 32.0)
     sim = oracle.PhysOracle(info, 0.56, np.float32)
     sim.step(2)  # warm-up
     steps, t0 = 0, time.perf_counter()
@@ -173,14 +180,15 @@ def cpu_baseline_sample(args, seconds_cap=15.0):
         el = time.perf_counter() - t0
         if el > seconds_cap or steps >= 5000:
             break
-    glups = args.nx * ny * steps / el / 1e9
+    glups = args.nx * args.ny * steps / el / 1e9
     return {"value": glups, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-            "sample": "oracle FP32 physics step on a %dx%d slice of the channel workload, %d steps, %.1f s"
-                      % (args.nx, ny, steps, el)}
+            "sample": "oracle FP32 physics step on the full %dx%d channel workload, %d steps after 2 warm-up "
+                      "steps, %.1f s" % (args.nx, args.ny, steps, el)}
 
 
 def run_reference(args):
-    """CPU restatement of the reference path (oracle), each step a bounded slice."""
+    """CPU restatement of the reference path (the oracle) on the full workload, all host
+    threads: W warm-up steps, then K timed steps."""
     import numpy as np
 
     import oracle
@@ -188,24 +196,120 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    ny = max(64, min(args.ny, int(os.environ.get("LBM_CPU_SAMPLE_ROWS", "512"))))
-    info, _ = oracle.mask_physics_channel(args.nx, ny, 0.05, 1234, 0.05, 8.0, 32.0)
+    info, _ = oracle.mask_physics_channel(args.nx, args.ny, 0.05, 1234, 0.05, 8.0, 32.0)
     sim = oracle.PhysOracle(info, 0.56, np.float32)
     sim.step(args.warmup)
     t0 = time.perf_counter()
     sim.step(args.steps)
     el = time.perf_counter() - t0
-    glups = args.nx * ny * args.steps / el / 1e9
+    glups = args.nx * args.ny * args.steps / el / 1e9
     cores = oracle.num_threads()
     line = {"impl": "reference", "metric": METRIC, "value": glups, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded channel mask)", "config": config_dict(args),
             "cpu_baseline": {"value": glups, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "oracle FP32 physics step on a %dx%d slice of the channel workload per step"
-                                       % (args.nx, ny)},
+                             "sample": "oracle FP32 physics step on the full %dx%d channel workload, %d steps"
+                                       % (args.nx, args.ny, args.steps)},
             "e2e": {"value": glups, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def timed_intervals(step_k, stream, steps, min_seconds, min_repeats=10, max_repeats=20000):
+    """Device milliseconds of R back-to-back intervals of `steps` steps (step_k(steps) queues
+    one interval), each bracketed by CUDA events on `stream`.  R >= min_repeats and large
+    enough that the intervals together last about min_seconds, estimated from a first
+    interval; one host synchronisation at the end."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step_k(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    est = max(e0.elapsed_time(e1), 1e-3)
+    reps = int(min(max_repeats, max(min_repeats, round(min_seconds * 1e3 / est))))
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, b in evs:
+        a.record(stream)
+        step_k(steps)
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def median(xs):
+    ys = sorted(xs)
+    n = len(ys)
+    return ys[n // 2] if n % 2 else 0.5 * (ys[n // 2 - 1] + ys[n // 2])
+
+
+def glups_of(cells, steps, ms):
+    return cells * steps / (ms * 1e-3) / 1e9
+
+
+def measure_sim(sim, stream, cells, bytes_per_cell, peak, steps=100, warmup=5, min_seconds=0.5):
+    """GLUPS (median over repeated intervals) and roofline fraction of one simulator."""
+    import torch
+
+    sim.set_stream(stream.cuda_stream)
+    sim.step(warmup)
+    torch.cuda.synchronize()
+    ms = timed_intervals(sim.step, stream, steps, min_seconds, min_repeats=3)
+    g = glups_of(cells, steps, median(ms))
+    return {"glups": g, "gb_per_s": g * bytes_per_cell, "roofline_frac": g * bytes_per_cell / peak,
+            "bytes_per_cell": bytes_per_cell, "steps_per_interval": steps, "intervals": len(ms),
+            "spread_glups": [glups_of(cells, steps, max(ms)), glups_of(cells, steps, min(ms))]}
+
+
+def run_extras(args, stream, peak):
+    """The other forms of the step at the precision form's size (8192^2), each timed on its own
+    lattice: the FP32 channel (the size the 80 % target is stated for), the reference's own
+    rules (its Poiseuille scene) in the fast and the exact arithmetic, 16-bit storage of the
+    channel (FP16 and BF16, round-to-nearest and stochastic rounding), and the batched form
+    (256 seeded domains, autotuned persistent launch against the per-domain loop)."""
+    import torch
+
+    from simuverse_gb300 import BatchSimulator, FluidSimulator, generate_domains
+
+    n = args.extras_size
+    cells = n * n
+    chan = dict(mode="physics", scene="channel", inlet_speed=0.05, solid_fraction=0.05, disk_radius=(8.0, 32.0),
+                seed=1234)
+    out = {"size": [n, n]}
+    forms = [("fp32", dict(chan, tau=0.56), 72),
+             ("reference_rules_fast", dict(mode="reference", scene="poiseuille", tau=0.56, arith="fast"), 72),
+             ("reference_rules_exact", dict(mode="reference", scene="poiseuille", tau=0.56, arith="exact"), 72),
+             ("f16", dict(chan, tau=0.6, dtype="f16"), 36),
+             ("f16_stochastic", dict(chan, tau=0.6, dtype="f16", rounding="stochastic"), 36),
+             ("bf16_stochastic", dict(chan, tau=0.6, dtype="bf16", rounding="stochastic"), 36)]
+    for name, kw, bpc in forms:
+        sim = FluidSimulator(n, n, **kw)
+        out[name] = measure_sim(sim, stream, cells, bpc, peak)
+        sim.close()
+        torch.cuda.synchronize()
+    for name in ("f16", "f16_stochastic", "bf16_stochastic"):
+        out[name]["over_fp32"] = out[name]["glups"] / out["fp32"]["glups"]
+
+    doms = generate_domains(256, 1234)
+    b = BatchSimulator(doms)
+    b.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    tuned = b.tune(trial_steps=10)
+    res = {"domains": len(doms), "cells": b.cells, "tune_seconds": time.perf_counter() - t0, "tuned": tuned}
+    for method, steps in (("persistent", 200), ("domain_loop", 50)):
+        b.configure(method=method)
+        b.step(3)
+        b.status()
+        ms = timed_intervals(b.step, stream, steps, 0.3, min_repeats=3)
+        b.status()
+        g = glups_of(b.cells, steps, median(ms))
+        res[method] = {"glups": g, "gb_per_s": 72 * g, "roofline_frac": 72 * g / peak, "steps_per_interval": steps,
+                       "intervals": len(ms)}
+    res["persistent_over_loop"] = res["persistent"]["glups"] / res["domain_loop"]["glups"]
+    b.close()
+    out["batch"] = res
+    return out
 
 
 def run_gpu(args):
@@ -234,24 +338,22 @@ def run_gpu(args):
     sim.step(args.warmup)
     torch.cuda.synchronize()
 
-    # ---- timed region: K steps, device time on the launching stream
+    # ---- timed region: R intervals of exactly K steps each, device time on the launching
+    # stream; R repeats the interval until about --min-seconds of load, so the clock samples
+    # see the kernel running
     clocks = ClockSampler(local)
     clocks.start()
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
     launches0 = sim.kernel_launches
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    sim.step(args.steps)
-    ev1.record(stream)
+    ms_list = timed_intervals(sim.step, stream, args.steps, args.min_seconds)
     torch.cuda.synchronize()
     if pg:
         pg.barrier()
-    ms = ev0.elapsed_time(ev1)
     gpu_launches = sim.kernel_launches - launches0
     clk = clocks.stop()
+    ms = median(ms_list)
     ms_max = max_over_ranks(pg, ms, "cuda")
     value = replica_glups(world, cells, args.steps, ms_max * 1e-3)
     per_launch_s = ms * 1e-3 / args.steps
@@ -265,31 +367,20 @@ def run_gpu(args):
     sim_m.set_stream(stream.cuda_stream)
     sim_m.step(args.warmup)
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        sim_m.step(1)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    glups_macro = cells * args.steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    glups_macro = glups_of(cells, args.steps, median(timed_intervals(sim_m.step, stream, args.steps, 0.3,
+                                                                        min_repeats=3)))
     sim_m.close()
     sim.close()
     torch.cuda.synchronize()
 
     # ---- the reference's own rules (reference mode, its Poiseuille scene) at the same size
-    glups_ref_mode = None
+    glups_ref_mode = {}
     if args.dtype == "f32":
-        sim_r = FluidSimulator(args.nx, args.ny, mode="reference", scene="poiseuille", tau=0.56)
-        sim_r.set_stream(stream.cuda_stream)
-        sim_r.step(args.warmup)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        sim_r.step(args.steps)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        glups_ref_mode = cells * args.steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
-        sim_r.close()
+        for arith in ("fast", "exact"):
+            sim_r = FluidSimulator(args.nx, args.ny, mode="reference", scene="poiseuille", tau=0.56, arith=arith)
+            glups_ref_mode[arith] = measure_sim(sim_r, stream, cells, 72, peak, steps=args.steps, warmup=args.warmup,
+                                                min_seconds=0.3)["glups"]
+            sim_r.close()
 
     # ---- end to end through the public API, host buffers
     if pg:
@@ -310,26 +401,38 @@ def run_gpu(args):
     h2d = 24 * len(scene_disks(**params))  # the channel's disk list; the mask is built on the device
     d2h = cells * 12  # rho, ux, uy read back
 
+    extras = None
+    if world == 1 and not args.no_extras:
+        extras = run_extras(args, stream, peak)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
             "data": "synthetic (seeded channel mask, equilibrium start)", "config": config_dict(args),
+            "repeats": len(ms_list),
+            "spread": {"glups_min": glups_of(cells, args.steps, max(ms_list)),
+                       "glups_max": glups_of(cells, args.steps, min(ms_list)),
+                       "what": "value is the median over `repeats` back-to-back intervals of `steps` steps"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": (tr or {}).get("bytes_per_launch_scaled"),
                          "traffic_source": (tr or {}).get("source"),
                          "algorithmic_bytes_per_launch": bytes_per_cell * cells},
             "macro_every_step_glups": glups_macro,
-            "reference_mode_glups": glups_ref_mode,
+            "reference_mode_glups": glups_ref_mode.get("fast"),
+            "reference_mode_exact_glups": glups_ref_mode.get("exact"),
             "e2e": {"value": e2e_glups, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps,
                     "what": "create (disk list upload, scene mask built on the device) + K steps + macro "
                             "read-back into page-locked host buffers, wall clock"},
             "gpu_launches": gpu_launches,
+            "gpu_launches_per_interval": gpu_launches // max(1, len(ms_list) + 1),
             "clocks": clk,
         }
+        if extras is not None:
+            line["extras"] = extras
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample(args)
         print(json.dumps(line), flush=True)
@@ -598,6 +701,10 @@ def main():
     ap.add_argument("--ny", type=int, default=4096)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f16", "bf16", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the 8192^2 forms and the batched form")
+    ap.add_argument("--extras-size", type=int, default=8192)
+    ap.add_argument("--min-seconds", type=float, default=2.0,
+                    help="repeat the K-step interval until about this much device time is timed")
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2", "tiled"])
     ap.add_argument("--rounding", default="nearest", choices=["nearest", "stochastic"],
                     help="rounding of 16-bit population stores")

@@ -108,6 +108,16 @@ extern "C" {
                                       (reproducible).  Runs on LBM_KERNEL_TILED, _VEC2 and
                                       _CELL (AUTO picks as for round-to-nearest). */
 
+/* reference mode: floating-point evaluation of the shader rules (collide_stream.wgsl:40-87).
+   Both keep every rule of the reference -- truncated weights and clamp maxima (mod.rs:39-49),
+   the rho clamp (:49), the forcing rows' velocity replacement (:55-71), the population clamp
+   (:79-83), the wall-cell storage of boundary.wgsl:28-31 -- and differ only in rounding. */
+#define LBM_ARITH_EXACT 0 /* every WGSL operation rounded on its own (no multiply-add
+                             contraction, IEEE divisions): bit-identical to the oracle */
+#define LBM_ARITH_FAST 1  /* multiply-adds contracted, one reciprocal of rho, the
+                             equilibrium evaluated on opposite pairs: within 1e-5 relative
+                             of the exact form after one step, memory-bound speed */
+
 /* initial masks */
 #define LBM_SCENE_POISEUILLE 0 /* lattice.rs:62-83 (the only scene the reference UI builds) */
 #define LBM_SCENE_CAVITY 1     /* lattice.rs:52-61 (reference); moving-lid box (physics) */
@@ -150,7 +160,8 @@ typedef struct lbm_params {
     int32_t kernel;          /* LBM_KERNEL_*: step kernel variant (results agree to rounding) */
     int32_t collision;       /* physics mode: LBM_COLLISION_* */
     int32_t rounding;        /* LBM_ROUNDING_* (16-bit storage; NEAREST otherwise) */
-    int32_t reserved[3];
+    int32_t arith;           /* reference mode: LBM_ARITH_* (physics mode ignores it) */
+    int32_t reserved[2];
 } lbm_params;
 
 typedef struct lbm_handle lbm_handle;
@@ -258,7 +269,9 @@ int lbm_load(lbm_handle* h, const char* path);
    lbm_conservation (bit-identical for the same populations), computed over device
    buffers the caller owns: d_populations in the storage format of (mode, dtype) -- 9
    planes of nx*ny values, absolute f for reference mode, f - w (FP16: times 2^10) for
-   physics mode -- d_info (device, nx*ny records; needed in physics mode to skip solids),
+   physics mode; the tiled 16-bit layout of LBM_KERNEL_TILED is not accepted (its sums would
+   be wrong without an error), so take such state from a handle with the SoA layout --
+   d_info (device, nx*ny records; needed in physics mode to skip solids),
    d_out (device, 3 doubles).  For callers that cannot allocate device memory: a host
    application whose own runtime owns every device buffer, a process whose device memory
    is claimed by another allocator's pool, or a real-time loop that cannot afford
@@ -266,7 +279,10 @@ int lbm_load(lbm_handle* h, const char* path);
    scratch is a fixed 29,184-byte array (1216 x 3 doubles) that every GPU loading the
    library keeps until exit.  Limit: lattices up to 2^30 cells (larger ones are rejected
    with LBM_ERR_ARG).  The first call on a device resolves the scratch address on that
-   device (make it before any stream capture).  Calls share the scratch: calls that overlap
+   device (make it before any stream capture) and keeps it for the life of the process: it
+   belongs to the device's primary context, the one the CUDA runtime uses, so the calls
+   must run with that context current, and a cudaDeviceReset invalidates the kept address
+   (do not call this entry point after one).  Calls share the scratch: calls that overlap
    on the GPU race.  Asynchronous on cuda_stream (NULL: the legacy default stream). */
 int lbm_conservation_noalloc(const void* d_populations, int32_t dtype, int32_t mode, const lbm_lattice_info* d_info,
                              int32_t nx, int32_t ny, double* d_out, void* cuda_stream);
@@ -283,6 +299,11 @@ int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches);
    macro: 3 planes of N floats (rho, ux, uy).  No counterpart in the reference, whose
    consumers bind macro_tex directly. */
 int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy);
+/* the population buffer the next step reads, in the handle's storage format (see
+   lbm_conservation_noalloc), valid until the next lbm_step, reset, load or destroy; *tiled
+   (may be NULL) = 1 when it is in the tiled 16-bit layout of LBM_KERNEL_TILED, 0 for the
+   plane-major SoA layout.  No counterpart in the reference. */
+int lbm_device_populations(lbm_handle* h, void** d_state, int32_t* tiled);
 
 /* ---------------------------------------------------------------------------------
    Consumers of the macro field, on the device (no texture or graphics interop).  Each

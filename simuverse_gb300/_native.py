@@ -29,6 +29,7 @@ SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4
 KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3, "vec2": 4, "tiled": 5}
 COLLISIONS = {"bgk": 0, "regularized": 1, "mrt": 2, "kbc": 3}
 ROUNDINGS = {"nearest": 0, "stochastic": 1}
+ARITHS = {"exact": 0, "fast": 1}
 BULK, BOUNDARY, INLET, OBSTACLE, OUTLET, EXTERNAL_FORCE, GHOST = 1, 2, 3, 4, 5, 6, 7
 
 # LatticeInfo (simuverse/src/fluid/lattice.rs:5-13)
@@ -44,7 +45,7 @@ class LbmParams(ctypes.Structure):
         ("seed", ctypes.c_uint64),
         ("pixel_size", ctypes.c_int32), ("macro_every_step", ctypes.c_int32),
         ("kernel", ctypes.c_int32), ("collision", ctypes.c_int32), ("rounding", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("arith", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
     ]
 
 
@@ -160,6 +161,7 @@ _SIGNATURES = {
     "lbm_steps_done": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_kernel_launches": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_device_macro": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "lbm_device_populations": [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_int32)],
     "lbm_batch_generate": [_I, ctypes.c_uint64, _P],
     "lbm_batch_create": [_I, _P, ctypes.POINTER(_P)],
     "lbm_batch_destroy": [_P],

@@ -267,6 +267,7 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "reference mode is BGK only");
     if (p.rounding != LBM_ROUNDING_NEAREST && p.rounding != LBM_ROUNDING_STOCHASTIC)
         return fail(LBM_ERR_ARG, "unknown rounding %d", p.rounding);
+    if (p.arith != LBM_ARITH_EXACT && p.arith != LBM_ARITH_FAST) return fail(LBM_ERR_ARG, "unknown arith %d", p.arith);
     if (p.rounding == LBM_ROUNDING_STOCHASTIC) {
         if (p.mode != LBM_MODE_PHYSICS || (p.dtype != LBM_DTYPE_F16 && p.dtype != LBM_DTYPE_BF16))
             return fail(LBM_ERR_ARG, "stochastic rounding applies to physics-mode FP16 / BF16 storage");
@@ -1049,6 +1050,13 @@ int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy) {
     if (rho) *rho = h->d_macro;
     if (ux) *ux = h->d_macro + h->N;
     if (uy) *uy = h->d_macro + 2 * h->N;
+    return LBM_OK;
+}
+
+int lbm_device_populations(lbm_handle* h, void** d_state, int32_t* tiled) {
+    LBM_TRY(check_handle(h));
+    if (d_state) *d_state = h->buf[h->cur];
+    if (tiled) *tiled = h->tiled ? 1 : 0;
     return LBM_OK;
 }
 

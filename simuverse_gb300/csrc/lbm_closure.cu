@@ -456,13 +456,17 @@ int pack(lbm_closure* c) {
 template <int CIN, int COUT, int EPI, bool PER>
 int conv(lbm_closure* c, const __nv_bfloat16* in, void* out, const __nv_bfloat16* w, const float* bias,
          const __nv_bfloat16* mask, int nimg, int H, int W) {
-    static bool attr = false;
     constexpr size_t smem = cl::conv_smem_bytes<CIN, COUT>();
-    if (!attr) {
-        C_CK(cudaFuncSetAttribute(cl::k_conv3x3<CIN, COUT, EPI, PER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-        attr = true;
-    }
+    static lbm::PerDevice<bool> attr;  // the attribute is set per device (c's device is current)
+    bool done = false;
+    C_CK(attr.get(
+        c->device,
+        [](bool& v) {
+            v = true;
+            return cudaFuncSetAttribute(cl::k_conv3x3<CIN, COUT, EPI, PER>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        },
+        &done));
     const dim3 grid((unsigned)((W + cl::CONV_CELLS - 1) / cl::CONV_CELLS), (unsigned)((H + cl::CONV_ROWS - 1) / cl::CONV_ROWS),
                     (unsigned)nimg);
     cl::k_conv3x3<CIN, COUT, EPI, PER><<<grid, 32 * cl::CONV_WARPS, smem, c->stream>>>(in, out, w, bias, mask, H, W);

@@ -6,6 +6,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -60,6 +61,33 @@ struct lbm_handle {
 };
 
 namespace lbm {
+
+// Launch set-up that belongs to one device: function attributes are set per device context
+// and SM counts may differ between devices.  PerDevice<T> keeps one T per device ordinal,
+// filled once by the caller's set-up under a mutex (thread-safe, each device on its own).
+constexpr int MAX_DEVICES = 64;
+template <class T>
+struct PerDevice {
+    std::mutex mu;
+    T val[MAX_DEVICES] = {};
+    bool ready[MAX_DEVICES] = {};
+    // the device's value, running setup(T&) -> cudaError_t the first time; an error leaves
+    // the device not set up (the next call tries again)
+    template <class F>
+    cudaError_t get(int dev, F setup, T* out) {
+        if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!ready[dev]) {
+            T v{};
+            const cudaError_t e = setup(v);
+            if (e != cudaSuccess) return e;
+            val[dev] = v;
+            ready[dev] = true;
+        }
+        *out = val[dev];
+        return cudaSuccess;
+    }
+};
 
 constexpr int TPB = 128;          // threads per block along x for the step kernels
 constexpr int RED_BLOCKS = 1216;  // 8 x 152 SMs; fixed so FP64 sums have a fixed order

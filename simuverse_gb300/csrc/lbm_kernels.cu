@@ -204,9 +204,22 @@ __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __re
 
 // ------------------------------------------------------------------------------------
 // reference-mode step: collide_stream.wgsl:25-88 + boundary.wgsl:3-35, one pass
+//
+// FAST = false (LBM_ARITH_EXACT): every WGSL operation rounded on its own, bit-identical to
+// the oracle.  FAST = true (LBM_ARITH_FAST): the same rules -- truncated weights and maxima,
+// rho clamp, forcing rows, population clamp, wall-cell storage -- with the moments summed as
+// a tree, one correctly rounded reciprocal of rho instead of the IEEE divisions, the
+// equilibrium of each opposite pair (j, inv j) split into the part even in e,
+// rho w (1 - 1.5 u.u + 4.5 (e.u)^2), and the odd part 3 rho w (e.u), and multiply-adds left
+// to the compiler: about half the instructions, so the step runs at memory speed.
 // ------------------------------------------------------------------------------------
-template <bool MACRO, class IDX>
-__global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, float* __restrict__ B,
+// resident blocks of TPB threads per SM the fast reference-mode step is compiled for (16: 32
+// registers, full occupancy)
+#ifndef LBM_REF_FAST_MIN_BLOCKS
+#define LBM_REF_FAST_MIN_BLOCKS 16
+#endif
+template <bool MACRO, class IDX, bool FAST>
+__global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref_step(const float* __restrict__ A, float* __restrict__ B,
                                                   uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                   float omega, int nx, int ny, float* __restrict__ macro) {
     const int x = blockIdx.x * TPB + threadIdx.x;
@@ -236,25 +249,34 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
         const IDX row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
         f[j] = __ldg(A + (row + (IDX)sx + (IDX)j * N));
     }
-    // collide_stream.wgsl:40-48.  The terms e * f with e = 0 add a zero and those with e = +-1
-    // add or subtract f exactly, so they are written as such (populations are finite and
-    // clamped to [0, max], so the values are those of the literal expressions; only the sign of
-    // an exact zero may differ)
-    float rho = 0.0f, vx = 0.0f, vy = 0.0f;
+    // collide_stream.wgsl:40-48
+    float rho = 0.0f, vx = 0.0f, vy = 0.0f, inv = 0.0f;
+    if constexpr (FAST) {
+        rho = f[0] + (((f[1] + f[3]) + (f[2] + f[4])) + ((f[5] + f[7]) + (f[6] + f[8])));
+        const float jx = (f[1] - f[3]) + ((f[5] - f[7]) + (f[8] - f[6]));
+        const float jy = (f[4] - f[2]) + ((f[7] - f[5]) + (f[8] - f[6]));
+        rho = fminf(fmaxf(rho, 0.8f), 1.2f);
+        inv = __frcp_rn(rho);
+        vx = jx * inv;
+        vy = jy * inv;
+    } else {
+        // the terms e * f with e = 0 add a zero and those with e = +-1 add or subtract f
+        // exactly, so they are written as such (populations are finite and clamped to
+        // [0, max], so the values are those of the literal expressions; only the sign of an
+        // exact zero may differ)
 #pragma unroll
-    for (int j = 0; j < 9; ++j) {
-        rho = __fadd_rn(rho, f[j]);
-        if (EX(j) == 1) vx = __fadd_rn(vx, f[j]);
-        if (EX(j) == -1) vx = __fsub_rn(vx, f[j]);
-        if (EY(j) == 1) vy = __fadd_rn(vy, f[j]);
-        if (EY(j) == -1) vy = __fsub_rn(vy, f[j]);
+        for (int j = 0; j < 9; ++j) {
+            rho = __fadd_rn(rho, f[j]);
+            if (EX(j) == 1) vx = __fadd_rn(vx, f[j]);
+            if (EX(j) == -1) vx = __fsub_rn(vx, f[j]);
+            if (EY(j) == 1) vy = __fadd_rn(vy, f[j]);
+            if (EY(j) == -1) vy = __fsub_rn(vy, f[j]);
+        }
+        rho = fminf(fmaxf(rho, 0.8f), 1.2f);
+        vx = __fdiv_rn(vx, rho);
+        vy = __fdiv_rn(vy, rho);
     }
-    rho = fminf(fmaxf(rho, 0.8f), 1.2f);
-    vx = __fdiv_rn(vx, rho);
-    vy = __fdiv_rn(vy, rho);
-    float F[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) F[j] = 0.0f;
+    float fx = 0.0f, fy = 0.0f;  // the forcing term F_j = 3 w_j (e_j . f) is 0 unless a force acts
     if (!fast && (m == LBM_INLET || m == LBM_EXTERNAL_FORCE)) {  // collide_stream.wgsl:55-71
         lbm_lattice_info in = info[c];
         if (in.block_iter > 0) {
@@ -265,34 +287,65 @@ __global__ void __launch_bounds__(TPB) k_ref_step(const float* __restrict__ A, f
             }
             info[c] = in;
         }
-        const float fx = in.vx, fy = in.vy;
-        vx = __fdiv_rn(__fmul_rn(fx, 0.5f), rho);
-        vy = __fdiv_rn(__fmul_rn(fy, 0.5f), rho);
-#pragma unroll
-        for (int j = 0; j < 9; ++j)
-            F[j] = __fmul_rn(__fmul_rn(REF_W(j), 3.0f),
-                             __fadd_rn(__fmul_rn((float)EX(j), fx), __fmul_rn((float)EY(j), fy)));
+        fx = in.vx;
+        fy = in.vy;
+        if constexpr (FAST) {
+            vx = (0.5f * fx) * inv;
+            vy = (0.5f * fy) * inv;
+        } else {
+            vx = __fdiv_rn(__fmul_rn(fx, 0.5f), rho);
+            vy = __fdiv_rn(__fmul_rn(fy, 0.5f), rho);
+        }
     }
     if (MACRO) { macro[c] = rho; macro[c + N] = vx; macro[c + 2 * N] = vy; }
-    const float usqr = __fmul_rn(1.5f, __fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)));
+    float t[9];
+    if constexpr (FAST) {
+        // t_j = (1 - omega) f_j + omega feq_j, feq of the pair (j, k = inv j) = sym +- asy
+        const float usqr = 1.5f * (vx * vx + vy * vy);
+        const float base = 1.0f - usqr, om1 = 1.0f - omega;
+        const float ow0 = omega * (rho * REF_W(0)), ow1 = omega * (rho * REF_W(1)), ow5 = omega * (rho * REF_W(5));
+        t[0] = om1 * f[0] + ow0 * base;
+        auto pair = [&](int j, int k, float eu, float ow) {
+            const float sym = ow * (base + (4.5f * eu) * eu);
+            const float asy = (3.0f * ow) * eu;
+            t[j] = om1 * f[j] + (sym + asy);
+            t[k] = om1 * f[k] + (sym - asy);
+        };
+        pair(1, 3, vx, ow1);
+        pair(4, 2, vy, ow1);
+        pair(8, 6, vx + vy, ow5);
+        pair(5, 7, vx - vy, ow5);
+    } else {
+        const float usqr = __fmul_rn(1.5f, __fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)));
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            // e . u with e_x, e_y in {-1, 0, 1}: the same value as the literal products and sum
+            const float ex = EX(j) == 1 ? vx : (EX(j) == -1 ? -vx : 0.0f);
+            const float ey = EY(j) == 1 ? vy : (EY(j) == -1 ? -vy : 0.0f);
+            const float eu = (EX(j) == 0) ? ey : ((EY(j) == 0) ? ex : __fadd_rn(ex, ey));
+            const float feq = __fmul_rn(
+                __fmul_rn(rho, REF_W(j)),
+                __fsub_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(3.0f, eu)), __fmul_rn(4.5f, __fmul_rn(eu, eu))), usqr));
+            t[j] = __fsub_rn(f[j], __fmul_rn(omega, __fsub_rn(f[j], feq)));
+        }
+    }
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
-        // e . u with e_x, e_y in {-1, 0, 1}: the same value as the literal products and sum
-        const float ex = EX(j) == 1 ? vx : (EX(j) == -1 ? -vx : 0.0f);
-        const float ey = EY(j) == 1 ? vy : (EY(j) == -1 ? -vy : 0.0f);
-        const float eu = (EX(j) == 0) ? ey : ((EY(j) == 0) ? ex : __fadd_rn(ex, ey));
-        const float feq = __fmul_rn(__fmul_rn(rho, REF_W(j)),
-                                    __fsub_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(3.0f, eu)), __fmul_rn(4.5f, __fmul_rn(eu, eu))),
-                                              usqr));
-        float t = __fsub_rn(f[j], __fmul_rn(omega, __fsub_rn(f[j], feq)));
-        if (!fast) t = __fadd_rn(t, F[j]);  // + 0 when no force acts (the value is unchanged)
-        if (t > REF_MAX(j)) t = REF_MAX(j);
-        else if (t < 0.0f) t = 0.0f;
+        float v = t[j];
+        if (!fast) {  // + F_j (+-0 when no force acts: the value is unchanged)
+            if constexpr (FAST)
+                v = v + (3.0f * REF_W(j)) * ((float)EX(j) * fx + (float)EY(j) * fy);
+            else
+                v = __fadd_rn(v, __fmul_rn(__fmul_rn(REF_W(j), 3.0f),
+                                           __fadd_rn(__fmul_rn((float)EX(j), fx), __fmul_rn((float)EY(j), fy))));
+        }
+        if (v > REF_MAX(j)) v = REF_MAX(j);  // collide_stream.wgsl:79-83
+        else if (v < 0.0f) v = 0.0f;
         if (!fast && (fl & (1u << (FL_DIR_SHIFT + j)))) {
-            B[c + (IDX)(EY(j) * nx + EX(j)) + (IDX)INV(j) * N] = t;
+            B[c + (IDX)(EY(j) * nx + EX(j)) + (IDX)INV(j) * N] = v;
             B[c + (IDX)j * N] = 0.0f;
         } else {
-            B[c + (IDX)j * N] = t;
+            B[c + (IDX)j * N] = v;
         }
     }
 }
@@ -628,24 +681,21 @@ static cudaError_t phys_step_t(lbm_handle* h, cudaStream_t s) {
     }
 }
 
+template <bool MACRO, class IDX, bool FAST>
+static cudaError_t ref_step_t(lbm_handle* h, cudaStream_t s) {
+    k_ref_step<MACRO, IDX, FAST><<<cell_grid(h), TPB, 0, s>>>((const float*)h->buf[h->cur], (float*)h->buf[h->cur ^ 1],
+                                                              h->d_flags, h->d_info, h->omega, h->nx, h->ny, h->d_macro);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
     if (h->p.mode == LBM_MODE_REFERENCE) {
-        const float* A = (const float*)h->buf[h->cur];
-        float* B = (float*)h->buf[h->cur ^ 1];
         const bool idx32 = (size_t)9 * h->N < ((size_t)1 << 32);
-        if (write_macro && idx32)
-            k_ref_step<true, uint32_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
-                                                                    h->d_macro);
-        else if (write_macro)
-            k_ref_step<true, size_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
-                                                                  h->d_macro);
-        else if (idx32)
-            k_ref_step<false, uint32_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
-                                                                     h->d_macro);
-        else
-            k_ref_step<false, size_t><<<cell_grid(h), TPB, 0, s>>>(A, B, h->d_flags, h->d_info, h->omega, h->nx, h->ny,
-                                                                   h->d_macro);
-        return cudaGetLastError();
+        if (h->p.arith == LBM_ARITH_FAST)
+            return idx32 ? (write_macro ? ref_step_t<true, uint32_t, true>(h, s) : ref_step_t<false, uint32_t, true>(h, s))
+                         : (write_macro ? ref_step_t<true, size_t, true>(h, s) : ref_step_t<false, size_t, true>(h, s));
+        return idx32 ? (write_macro ? ref_step_t<true, uint32_t, false>(h, s) : ref_step_t<false, uint32_t, false>(h, s))
+                     : (write_macro ? ref_step_t<true, size_t, false>(h, s) : ref_step_t<false, size_t, false>(h, s));
     }
     // auto = the fastest variant measured on GB300: one cell per thread for FP32 and FP64
     // (94.9 % of the HBM copy bandwidth at 4096^2 FP32, against 70.9 % for VEC4 and 68.6 % for

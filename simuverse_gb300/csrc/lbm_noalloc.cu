@@ -16,7 +16,9 @@
 // library keeps until the process exits.  Host code cannot use the array's name as a
 // device address (on the host it names a stand-in object), so the first call on each
 // device resolves the address with cudaGetSymbolAddress, with that device current, and
-// caches it; make that first call before any stream capture.  Each call overwrites all
+// caches it; make that first call before any stream capture.  The cached address belongs to
+// the device's primary context (the CUDA runtime's): calls must run with that context
+// current, and a cudaDeviceReset, which destroys it, invalidates the cache.  Each call overwrites all
 // NOALLOC_BLOCKS partial triples before the final pass reads them, so nothing has to be
 // cleared between calls.  All calls share the one array: two calls whose kernels overlap
 // on the GPU (for example on two streams) race on it and may return wrong sums.

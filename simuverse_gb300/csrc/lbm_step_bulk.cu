@@ -355,18 +355,28 @@ static cudaError_t bulk_t(lbm_handle* h, cudaStream_t s) {
     using T = typename ST::T;
     using R = typename ST::R;
     using L = BulkLayout<ST>;
-    static int blocks_per_sm = 0;
-    static int sms = 0;
-    if (blocks_per_sm == 0) {
-        cudaError_t e = cudaFuncSetAttribute(k_phys_step_bulk<ST, MACRO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             L::SMEM);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_phys_step_bulk<ST, MACRO>, BULK_TPB,
-                                                               L::SMEM);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-        if (e != cudaSuccess) return e;
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
+    // per device (the handle's device is current): the shared-memory attribute, resident
+    // blocks per SM and the SM count
+    struct Setup {
+        int blocks_per_sm, sms;
+    };
+    static PerDevice<Setup> per_device;
+    Setup su{};
+    cudaError_t e = per_device.get(
+        h->device,
+        [&](Setup& v) {
+            cudaError_t r = cudaFuncSetAttribute(k_phys_step_bulk<ST, MACRO>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, L::SMEM);
+            if (r == cudaSuccess)
+                r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v.blocks_per_sm, k_phys_step_bulk<ST, MACRO>,
+                                                                  BULK_TPB, L::SMEM);
+            if (r == cudaSuccess) r = cudaDeviceGetAttribute(&v.sms, cudaDevAttrMultiProcessorCount, h->device);
+            if (v.blocks_per_sm < 1) v.blocks_per_sm = 1;
+            return r;
+        },
+        &su);
+    if (e != cudaSuccess) return e;
+    const int blocks_per_sm = su.blocks_per_sm, sms = su.sms;
     const R omega = sizeof(R) == 8 ? (R)h->omega_d : (R)h->omega;
     const long ntiles = (long)((h->nx + BULK_TW - 1) / BULK_TW) * h->ny;
     const long grid = std::min<long>(ntiles, (long)blocks_per_sm * sms);

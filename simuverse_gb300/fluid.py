@@ -31,7 +31,7 @@ def make_params(nx: int, ny: int, *, mode: str = "reference", dtype: str = "f32"
                 tau: float = None, viscosity: float = None, lid_speed: float = None, inlet_speed: float = None,
                 solid_fraction: float = 0.05, disk_radius=(8.0, 32.0), seed: int = 0, pixel_size: int = 2,
                 macro_every_step: bool = False, kernel: str = "auto", collision: str = "bgk",
-                rounding: str = "nearest") -> "nat.LbmParams":
+                rounding: str = "nearest", arith: str = "exact") -> "nat.LbmParams":
     """lbm_params from keyword arguments (lbm_params_default for the rest)."""
     lib = nat.load()
     p = nat.LbmParams()
@@ -56,6 +56,7 @@ def make_params(nx: int, ny: int, *, mode: str = "reference", dtype: str = "f32"
     p.kernel = nat.KERNELS[kernel]
     p.collision = nat.COLLISIONS[collision]
     p.rounding = nat.ROUNDINGS[rounding]
+    p.arith = nat.ARITHS[arith]
     return p
 
 
@@ -78,7 +79,7 @@ class FluidSimulator:
         ("reference" | "physics"), dtype ("f32" | "f64" | "f16" | "bf16"), scene ("poiseuille" |
         "cavity" | "custom" | "channel" | "periodic"), tau or viscosity, lid_speed, inlet_speed,
         solid_fraction, disk_radius, seed, pixel_size, macro_every_step, kernel, collision,
-        rounding ("nearest" | "stochastic")."""
+        rounding ("nearest" | "stochastic"), arith ("exact" | "fast": reference-mode rounding)."""
         lib = nat.load()
         p = make_params(nx, ny, **kw)
         mode, dtype, scene = kw.get("mode", "reference"), kw.get("dtype", "f32"), kw.get("scene", "poiseuille")
@@ -274,6 +275,13 @@ class FluidSimulator:
         n = ctypes.c_uint64(0)
         nat.check(self._lib.lbm_kernel_launches(self._h, ctypes.byref(n)))
         return int(n.value)
+
+    def device_populations(self):
+        """(device pointer, tiled) of the population buffer the next step reads, in the
+        handle's storage format; valid until the next step, reset, load or close."""
+        p, t = ctypes.c_void_p(), ctypes.c_int32()
+        nat.check(self._lib.lbm_device_populations(self._h, ctypes.byref(p), ctypes.byref(t)))
+        return p.value, bool(t.value)
 
     def device_macro(self):
         """Device pointers (rho, ux, uy) of the macro planes, for in-GPU consumers."""

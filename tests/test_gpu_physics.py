@@ -199,10 +199,10 @@ def test_bulk_kernel_matches_cell_kernel(gpu, scene, nx, ny, dtype):
         assert np.max(np.abs(x - y)[fluid]) <= 10 * tol
 
 
-@pytest.mark.parametrize("collision", ["regularized", "mrt"])
+@pytest.mark.parametrize("collision", ["regularized", "mrt", "kbc"])
 def test_collision_variants_match_oracle(gpu, collision):
     nx, ny = 96, 80
-    code = {"regularized": 1, "mrt": 2}[collision]
+    code = {"regularized": 1, "mrt": 2, "kbc": 3}[collision]
     sim = FluidSimulator(nx, ny, mode="physics", scene="cavity", tau=0.55, lid_speed=0.08, collision=collision)
     ref = oracle.PhysOracle(oracle.mask_physics_cavity(nx, ny, 0.08), 0.55, np.float32, collision=code)
     sim.step(1)
@@ -229,3 +229,79 @@ def test_read_macro_into_caller_buffers(gpu):
         assert np.array_equal(a, b)
     with pytest.raises(ValueError):
         sim.read_macro(out=(np.empty(5, np.float32),) * 3)
+
+
+def test_kbc_decaying_turbulence_matches_oracle(gpu):
+    """KBC at tau 0.5005 on a periodic decaying-turbulence field (the collision and the
+    regime of the learned-closure study): max relative error <= 1e-5 (velocity relative to
+    u_rms) after one step, relative L2 <= 1e-4 after 300 steps, mass and momentum kept to
+    1e-10 relative in FP64."""
+    from simuverse_gb300.turbulence import random_velocity
+
+    n = 256
+    ux, uy = random_velocity(n, 4242, k0=8.0, u_rms=0.04)
+    ux, uy = ux.astype(np.float32), uy.astype(np.float32)
+    sim = FluidSimulator(n, n, mode="physics", scene="periodic", tau=0.5005, collision="kbc")
+    sim.init_equilibrium(None, ux, uy)
+    ref = oracle.PhysOracle(oracle.mask_periodic(n, n), 0.5005, np.float32, collision=3)
+    ref.init_equilibrium(None, ux, uy)
+    c0 = sim.conservation()
+    sim.step(1)
+    ref.step(1)
+    e_rho, e_u = _macro_err(sim, ref, 0.04)
+    assert e_rho <= 1e-5 and e_u <= 1e-5
+    sim.step(299)
+    ref.step(299)
+    rho, ux1, uy1 = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(rho, r_rho) <= 1e-4
+    assert rel_l2(np.stack([ux1, uy1]), np.stack([r_ux, r_uy])) <= 1e-4
+    c1 = sim.conservation()
+    assert abs(c1[0] - c0[0]) / c0[0] <= 1e-10
+    assert abs(c1[1] - c0[1]) <= 1e-10 * c0[0] and abs(c1[2] - c0[2]) <= 1e-10 * c0[0]
+
+
+def test_channel_4096_parity_with_oracle(gpu):
+    """The benchmarked workload at full size: channel 4096^2, Zou-He inlet u = 0.05, outflow,
+    walls, disks r 8-32 at 5 % solid, seed 1234, tau 0.56.  Same mask as the oracle's, max
+    relative error <= 1e-5 after one step, relative L2 <= 1e-4 after 200 steps."""
+    n = 4096
+    kw = dict(inlet_speed=0.05, seed=1234, solid_fraction=0.05, disk_radius=(8.0, 32.0))
+    sim = FluidSimulator(n, n, mode="physics", scene="channel", tau=0.56, **kw)
+    info, ndisk = oracle.mask_physics_channel(n, n, 0.05, 1234, 0.05, 8.0, 32.0)
+    assert ndisk > 100
+    assert np.array_equal(sim.info(), info)
+    ref = oracle.PhysOracle(info, 0.56, np.float32)
+    sim.step(1)
+    ref.step(1)
+    e_rho, e_u = _macro_err(sim, ref, 0.05)
+    assert e_rho <= 1e-5 and e_u <= 1e-5
+    sim.step(199)
+    ref.step(199)
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(rho, r_rho) <= 1e-4
+    assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= 1e-4
+    sim.close()
+
+
+def test_bulk_kernel_handles_on_two_devices(gpu):
+    """The bulk-copy kernel's shared-memory attribute and grid size are set up per device: an
+    FP64 handle (about 76 KB of dynamic shared memory) steps on every visible device."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.device_count() < 2:
+        pytest.skip("one GPU visible")
+    prev = torch.cuda.current_device()
+    results = []
+    try:
+        for dev in (0, 1):
+            torch.cuda.set_device(dev)
+            s = FluidSimulator(136, 100, mode="physics", dtype="f64", scene="cavity", tau=0.58, lid_speed=0.1,
+                               kernel="bulk")
+            s.step(20)
+            s.status()
+            results.append(s.read_populations(np.float64))
+            s.close()
+    finally:
+        torch.cuda.set_device(prev)
+    assert np.array_equal(results[0], results[1])

@@ -190,3 +190,138 @@ def test_errors_do_not_abort(gpu):
     mass, jx, jy = sim.conservation()
     pops = sim.read_populations().astype(np.float64)
     assert abs(mass - pops.sum()) <= 1e-9 * pops.sum()
+
+
+# ---------------------------------------------------------------------------------------
+# LBM_ARITH_FAST: the reference's rules (truncated weights and maxima, rho clamp, forcing
+# rows, population clamp, wall-cell storage) with contracted arithmetic and one reciprocal
+# of rho.  Stated bounds against the oracle: max relative error <= 1e-5 on rho and u after
+# one step (u relative to max(|u|, 1e-3)); relative L2 <= 1e-5 of rho and of u after 1000
+# steps; populations within 1e-6 absolute after one step.
+# ---------------------------------------------------------------------------------------
+TOL_FAST_1STEP = 1e-5
+TOL_FAST_L2_1000 = 1e-5
+TOL_FAST_POP_1STEP = 1e-6
+
+
+def _fast_close_max(sim, ref, tol=TOL_FAST_1STEP):
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert max_rel_err(rho, r_rho, 1e-6) <= tol
+    assert max_rel_err(ux, r_ux, 1e-3) <= tol
+    assert max_rel_err(uy, r_uy, 1e-3) <= tol
+
+
+def _fast_close_l2(sim, ref, tol=TOL_FAST_L2_1000):
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(rho, r_rho) <= tol
+    assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= tol
+
+
+def test_fast_cavity_256_one_step_and_1000(gpu):
+    sim = FluidSimulator(256, 256, mode="reference", scene="cavity", tau=0.6, lid_speed=0.1, arith="fast")
+    ref = oracle.RefOracle(256, 256, "cavity", tau=0.6, lid_vx=0.1)
+    sim.step(1)
+    ref.step(1)
+    _fast_close_max(sim, ref)
+    keep = comparable_slots(ref.info)
+    assert np.max(np.abs(sim.read_populations()[keep] - ref.populations[keep])) <= TOL_FAST_POP_1STEP
+    assert np.array_equal(sim.info(), ref.info)
+    sim.step(999)
+    ref.step(999)
+    _fast_close_l2(sim, ref)
+    # the clamps hold in the fast form too
+    pops = sim.read_populations()
+    maxima = np.array([0.6, 0.2222, 0.2222, 0.2222, 0.2222, 0.1111, 0.1111, 0.1111, 0.1111], np.float32)
+    assert (pops >= 0).all() and (pops <= maxima[:, None, None]).all()
+    rho = sim.read_macro()[0]
+    fluid = ~np.isin(ref.info["material"], (2, 4))
+    assert (rho[fluid] >= np.float32(0.8)).all() and (rho[fluid] <= np.float32(1.2)).all()
+
+
+def test_fast_poiseuille_with_interaction(gpu):
+    """600x375 Poiseuille at tau 0.56 with a click, a drag (forcing cells with countdown) and
+    a viscosity change: the fast form within the stated bounds after 40 frames (80 steps);
+    the masks and countdowns identical."""
+    nx, ny = 600, 375
+    sim = FluidSimulator(nx, ny, mode="reference", scene="poiseuille", tau=0.56, pixel_size=4, arith="fast")
+    ref = oracle.RefOracle(nx, ny, "poiseuille", tau=0.56, pixel_size=4)
+    sim.step(1)
+    ref.step(1)
+    _fast_close_max(sim, ref)
+    for frame in range(40):
+        if frame == 5:
+            assert sim.on_click((1400.0, 700.0)) == (ref.on_click(1400.0, 700.0) == 0)
+        if 10 <= frame < 20:
+            pos = (900.0 + 23.0 * frame, 400.0 + 11.0 * frame)
+            assert sim.touch_move(pos) == ref.touch_move(pos)
+        if frame == 25:
+            sim.update_uniforms(0.05)
+            ref.update_uniforms(0.05)
+        sim.compute()
+        ref.compute()
+    assert np.array_equal(sim.info(), ref.info)
+    _fast_close_l2(sim, ref)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))), ids=os.path.basename)
+def test_fast_golden_fixture(gpu, path):
+    z = np.load(path)
+    scene = str(z["scene"])
+    ny, nx = z["info_in"].shape
+    kw = {}
+    if scene == "cavity":
+        kw["lid_speed"] = float(z["speed"])
+    if scene == "poiseuille":
+        kw["inlet_speed"] = float(z["speed"])
+    sim = FluidSimulator(nx, ny, mode="reference", scene=scene, tau=float(z["tau"]), arith="fast", **kw)
+    if str(z["edit"]) == "force":
+        sim.set_info(z["info_init"])
+    for s in range(int(z["steps"])):
+        if str(z["edit"]) == "obstacle" and s == 2:
+            sim.add_obstacle(32, 30)
+        sim.step(1)
+    rho, ux, uy = sim.read_macro()
+    assert max_rel_err(rho, z["macro"][..., 2], 1e-6) <= TOL_FAST_1STEP
+    assert max_rel_err(ux, z["macro"][..., 0], 1e-3) <= TOL_FAST_1STEP
+    assert max_rel_err(uy, z["macro"][..., 1], 1e-3) <= TOL_FAST_1STEP
+    keep = comparable_slots(z["info_out"])
+    assert np.max(np.abs(sim.read_populations()[keep] - z["pops"][keep])) <= TOL_FAST_POP_1STEP
+    assert np.array_equal(sim.info(), z["info_out"])
+
+
+@pytest.mark.parametrize("scene,nx,ny", [("custom", 5, 7), ("cavity", 129, 67), ("poiseuille", 131, 97)])
+def test_fast_odd_sizes(gpu, scene, nx, ny):
+    sim = FluidSimulator(nx, ny, mode="reference", scene=scene, tau=0.57, arith="fast")
+    ref = oracle.RefOracle(nx, ny, scene, tau=0.57)
+    sim.step(1)
+    ref.step(1)
+    _fast_close_max(sim, ref)
+    sim.step(24)
+    ref.step(24)
+    _fast_close_l2(sim, ref)
+    assert np.array_equal(sim.info(), ref.info)
+
+
+def test_fast_poiseuille_8192_against_exact(gpu):
+    """The benchmarked size: the reference's Poiseuille scene at 8192^2, fast form against the
+    exact form (bit-identical to the oracle) after 1 and 100 steps."""
+    n = 8192
+    a = FluidSimulator(n, n, mode="reference", scene="poiseuille", tau=0.56, arith="fast")
+    b = FluidSimulator(n, n, mode="reference", scene="poiseuille", tau=0.56)
+    a.step(1)
+    b.step(1)
+    ra, xa, ya = a.read_macro()
+    rb, xb, yb = b.read_macro()
+    assert max_rel_err(ra, rb, 1e-6) <= TOL_FAST_1STEP
+    assert max_rel_err(xa, xb, 1e-3) <= TOL_FAST_1STEP
+    assert max_rel_err(ya, yb, 1e-3) <= TOL_FAST_1STEP
+    a.step(99)
+    b.step(99)
+    ra, xa, ya = a.read_macro()
+    rb, xb, yb = b.read_macro()
+    assert rel_l2(ra, rb) <= TOL_FAST_L2_1000
+    assert rel_l2(np.stack([xa, ya]), np.stack([xb, yb])) <= TOL_FAST_L2_1000
+    a.close()
+    b.close()
