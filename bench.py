@@ -441,6 +441,26 @@ def run_gpu(args):
         pg.destroy_process_group()
 
 
+def run_reference_rules(args):
+    """The reference's own rules (reference mode, its Poiseuille scene at args.nx x args.ny,
+    tau 0.56) in one arithmetic (--arith): GLUPS over K steps, median of repeated intervals,
+    and the fraction of the HBM roofline at 72 B per cell update."""
+    import torch
+
+    from simuverse_gb300 import FluidSimulator
+
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    peak, peak_kind = measured_peak()
+    sim = FluidSimulator(args.nx, args.ny, mode="reference", scene="poiseuille", tau=0.56, arith=args.arith)
+    r = measure_sim(sim, stream, args.nx * args.ny, 72, peak, steps=args.steps, warmup=args.warmup,
+                    min_seconds=args.min_seconds)
+    sim.close()
+    r.update({"workload": "reference rules, Poiseuille %dx%d, tau 0.56, arith %s" % (args.nx, args.ny, args.arith),
+              "peak_gbs": peak, "peak_source": peak_kind})
+    print(json.dumps(r), flush=True)
+
+
 def run_precision(args):
     """Precision form at 8192^2: GLUPS of FP32 / FP16 / BF16 storage with each kernel
     variant, and the error of each against an FP64 run of the same channel at checkpoints up
@@ -708,7 +728,10 @@ def main():
     ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2", "tiled"])
     ap.add_argument("--rounding", default="nearest", choices=["nearest", "stochastic"],
                     help="rounding of 16-bit population stores")
-    ap.add_argument("--workload", default="channel", choices=["channel", "precision", "batch", "closure", "view"])
+    ap.add_argument("--workload", default="channel",
+                    choices=["channel", "reference", "precision", "batch", "closure", "view"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "exact"],
+                    help="--workload reference: arithmetic of the reference-rule step")
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snapshots", type=int, default=125)
     ap.add_argument("--interval", type=int, default=160)
@@ -741,6 +764,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "reference":
+        run_reference_rules(args)
     elif args.workload == "precision":
         run_precision(args)
     elif args.workload == "batch":

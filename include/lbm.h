@@ -287,6 +287,19 @@ int lbm_load(lbm_handle* h, const char* path);
 int lbm_conservation_noalloc(const void* d_populations, int32_t dtype, int32_t mode, const lbm_lattice_info* d_info,
                              int32_t nx, int32_t ny, double* d_out, void* cuda_stream);
 
+/* Bounds-checked builds -- no counterpart in the reference.  liblbm_bounds.so is this library
+   compiled with LBM_BOUNDS_CHECK: the step kernels (reference mode, the one-cell physics step,
+   the tiled 16-bit step, the bulk-copy step and the batched one-cell update) compare every
+   population, flag and info index with the extent of its buffer before the access; an index
+   outside it is counted with the first one's index, extent and access site, and the access is
+   skipped (loads give 0), so nothing traps.  lbm_bounds_report returns the count since the
+   last report on the current device (any pointer may be NULL) and clears it;
+   lbm_bounds_selftest launches one thread that evaluates an index equal to its extent, with no
+   memory access, so that the next report shows count 1 and site 99.  Both return
+   LBM_ERR_STATE in the normal build. */
+int lbm_bounds_report(uint64_t* count, uint64_t* first_index, uint64_t* first_limit, int32_t* first_site);
+int lbm_bounds_selftest(void);
+
 /* synchronises; LBM_ERR_TIMEOUT if a step kernel gave up on a bounded wait since creation
    -- no counterpart in the reference */
 int lbm_status(lbm_handle* h);

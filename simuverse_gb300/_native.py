@@ -10,7 +10,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "liblbm.so")
+# SIMUVERSE_LBM_VARIANT=bounds loads the bounds-checked build (liblbm_bounds.so) instead
+VARIANT = os.environ.get("SIMUVERSE_LBM_VARIANT") or None
+LIB_PATH = os.path.join(HERE, "_lib", "liblbm_bounds.so" if VARIANT == "bounds" else "liblbm.so")
 
 # status codes (lbm.h)
 LBM_OK = 0
@@ -162,6 +164,9 @@ _SIGNATURES = {
     "lbm_kernel_launches": [_P, ctypes.POINTER(ctypes.c_uint64)],
     "lbm_device_macro": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)],
     "lbm_device_populations": [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_int32)],
+    "lbm_bounds_report": [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                          ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)],
+    "lbm_bounds_selftest": [],
     "lbm_batch_generate": [_I, ctypes.c_uint64, _P],
     "lbm_batch_create": [_I, _P, ctypes.POINTER(_P)],
     "lbm_batch_destroy": [_P],

@@ -1053,6 +1053,45 @@ int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy) {
     return LBM_OK;
 }
 
+int lbm_bounds_report(uint64_t* count, uint64_t* first_index, uint64_t* first_limit, int32_t* first_site) {
+#ifdef LBM_BOUNDS_CHECK
+    lbm::BoundsRecord total{};
+    cudaError_t (*takes[])(lbm::BoundsRecord*) = {lbm::bounds_take_kernels, lbm::bounds_take_vec,
+                                                 lbm::bounds_take_bulk, lbm::bounds_take_batch};
+    for (auto take : takes) {
+        lbm::BoundsRecord r{};
+        LBM_CK(take(&r));
+        if (r.count && !total.count) {
+            total.index = r.index;
+            total.limit = r.limit;
+            total.site = r.site;
+        }
+        total.count += r.count;
+    }
+    if (count) *count = total.count;
+    if (first_index) *first_index = total.index;
+    if (first_limit) *first_limit = total.limit;
+    if (first_site) *first_site = total.site;
+    return LBM_OK;
+#else
+    (void)count;
+    (void)first_index;
+    (void)first_limit;
+    (void)first_site;
+    return fail(LBM_ERR_STATE, "not a bounds-checked build: load liblbm_bounds.so");
+#endif
+}
+
+int lbm_bounds_selftest(void) {
+#ifdef LBM_BOUNDS_CHECK
+    LBM_CK(lbm::bounds_selftest(nullptr));
+    LBM_CK(cudaDeviceSynchronize());
+    return LBM_OK;
+#else
+    return fail(LBM_ERR_STATE, "not a bounds-checked build: load liblbm_bounds.so");
+#endif
+}
+
 int lbm_device_populations(lbm_handle* h, void** d_state, int32_t* tiled) {
     LBM_TRY(check_handle(h));
     if (d_state) *d_state = h->buf[h->cur];

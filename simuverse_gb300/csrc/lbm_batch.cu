@@ -263,6 +263,10 @@ __global__ void k_batch_flags(const BatchDomain* __restrict__ doms, int ndom, co
     }
 }
 
+#ifdef LBM_BOUNDS_CHECK
+cudaError_t bounds_take_batch(BoundsRecord* out) { return bounds_take_local(out); }
+#endif
+
 }  // namespace lbm
 
 // =====================================================================================

@@ -295,10 +295,17 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
     const OFF N = (OFF)pitch * (OFF)ny;
     const unsigned c = (unsigned)y * (unsigned)pitch + (unsigned)x;  // cells < 2^31
     const OFF cc = cell_off + (OFF)c, mc = (OFF)3 * cell_off + (OFF)c;
-    const unsigned fl = flags[cc];
+    // ends of this lattice's ranges for the bounds-checked build (phys_collide's info and flag
+    // accesses use cc, checked here)
+    const unsigned long long end_c = (unsigned long long)cell_off + (unsigned long long)N;
+    const unsigned long long end_p = (unsigned long long)pop_off + 9ull * (unsigned long long)N;
+    const unsigned long long end_m = 3ull * (unsigned long long)cell_off + 3ull * (unsigned long long)N;
+    const unsigned fl = in_bounds(cc, end_c, BS_CELL_FLAGS) ? flags[cc] : 0u;
     const int m = (int)(fl & FL_MAT_MASK);
     if (is_solid(m)) {
-        if (MACRO) { macro[mc] = 0.0f; macro[mc + N] = 0.0f; macro[mc + 2 * N] = 0.0f; }
+        if (MACRO && in_bounds(mc + 2 * N, end_m, BS_CELL_MACRO)) {
+            macro[mc] = 0.0f; macro[mc + N] = 0.0f; macro[mc + 2 * N] = 0.0f;
+        }
         return;
     }
     const bool outlet = (m == LBM_OUTLET);
@@ -311,7 +318,8 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
         for (int j = 0; j < 9; ++j) {
             const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
             const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-            d[j] = ST::ldu(A + (pop_off + (OFF)j * N + (OFF)(row + (unsigned)sx)));
+            const OFF i = pop_off + (OFF)j * N + (OFF)(row + (unsigned)sx);
+            d[j] = in_bounds(i, end_p, BS_CELL_PULL) ? ST::ldu(A + i) : R(0);
         }
     } else {
 #pragma unroll
@@ -319,9 +327,11 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
             const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? (outlet ? x : xp) : x);
             const unsigned row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
             if (fl & (1u << (FL_DIR_SHIFT + j))) {
-                R v = ST::ldu(A + (pop_off + (OFF)INV(j) * N + (OFF)c));  // half-way bounce-back
-                if (fl & FL_MOVING) {
-                    const lbm_lattice_info si = info[cell_off + (OFF)(row + sx)];
+                const OFF ib = pop_off + (OFF)INV(j) * N + (OFF)c;  // half-way bounce-back
+                R v = in_bounds(ib, end_p, BS_CELL_PULL) ? ST::ldu(A + ib) : R(0);
+                const OFF is = cell_off + (OFF)(row + sx);
+                if ((fl & FL_MOVING) && in_bounds(is, end_c, BS_CELL_INFO)) {
+                    const lbm_lattice_info si = info[is];
                     const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
                     // rounded product, not an FMA: a contracted wall term leaves a
                     // systematic mass drift of ~1e-12 per step in FP32
@@ -329,20 +339,29 @@ __device__ __forceinline__ void phys_cell_update(const typename ST::T* __restric
                 }
                 d[j] = v;
             } else {
-                d[j] = ST::ldu(A + (pop_off + (OFF)j * N + (OFF)(row + (unsigned)sx)));
+                const OFF i = pop_off + (OFF)j * N + (OFF)(row + (unsigned)sx);
+                d[j] = in_bounds(i, end_p, BS_CELL_PULL) ? ST::ldu(A + i) : R(0);
             }
         }
     }
     R o[9], rho, ux, uy;
     phys_collide<R, COLL>(d, m, fl, (size_t)cc, flags, info, omega, o, rho, ux, uy, R(ST::UNIT));
-    if (MACRO) { macro[mc] = (float)rho; macro[mc + N] = (float)ux; macro[mc + 2 * N] = (float)uy; }
+    if (MACRO && in_bounds(mc + 2 * N, end_m, BS_CELL_MACRO)) {
+        macro[mc] = (float)rho; macro[mc + N] = (float)ux; macro[mc + 2 * N] = (float)uy;
+    }
     if (SR) {
         const uint32_t q = sr_hash(c ^ seed);
 #pragma unroll
-        for (int j = 0; j < 9; ++j) ST::stu_sr(B + (pop_off + (OFF)j * N + (OFF)c), o[j], q * sr_mul(j));
+        for (int j = 0; j < 9; ++j) {
+            const OFF i = pop_off + (OFF)j * N + (OFF)c;
+            if (in_bounds(i, end_p, BS_CELL_STORE)) ST::stu_sr(B + i, o[j], q * sr_mul(j));
+        }
     } else {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) ST::stu(B + (pop_off + (OFF)j * N + (OFF)c), o[j]);
+        for (int j = 0; j < 9; ++j) {
+            const OFF i = pop_off + (OFF)j * N + (OFF)c;
+            if (in_bounds(i, end_p, BS_CELL_STORE)) ST::stu(B + i, o[j]);
+        }
     }
 }
 

@@ -42,8 +42,10 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
     const uint32_t op = ((uint32_t)yp * tpr + tx) * TS + 2 * lane;
     const uint32_t c0 = (uint32_t)y * nx + x0;  // cell index (flags, info, macro)
 
+    // extents for the bounds-checked build: cells, population elements, macro elements
+    const unsigned long long NC = N, NP = 9ull * N, NM = 3ull * N;
     unsigned fl[2];
-    const unsigned fq = *reinterpret_cast<const unsigned*>(flags + c0);
+    const unsigned fq = in_bounds(c0 + 1ull, NC, BS_TILE_FLAGS) ? *reinterpret_cast<const unsigned*>(flags + c0) : 0u;
     fl[0] = fq & 0xffffu;
     fl[1] = fq >> 16;
 
@@ -54,19 +56,20 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
         const T* Pr = EY(j) == 1 ? Pm : (EY(j) == -1 ? Pp : P0);
-        R v[2];
-        Vec2<ST>::ld(Pr + j * W, v);
+        const long long pr = (long long)(Pr - A) + j * W;  // element index of the pair (checked build)
+        R v[2] = {R(0), R(0)};
+        if (in_bounds((unsigned long long)pr + 1ull, NP, BS_TILE_PULL)) Vec2<ST>::ld(Pr + j * W, v);
         if (EX(j) == 0) {
             d[j][0] = v[0];
             d[j][1] = v[1];
         } else if (EX(j) == 1) {  // source x - 1
             R prev = __shfl_up_sync(0xffffffffu, v[1], 1);
-            if (lane == 0) prev = ST::ldu(Pr + dl + j * W);
+            if (lane == 0) prev = in_bounds((unsigned long long)(pr + dl), NP, BS_TILE_PULL) ? ST::ldu(Pr + dl + j * W) : R(0);
             d[j][0] = prev;
             d[j][1] = v[0];
         } else {  // source x + 1
             R next = __shfl_down_sync(0xffffffffu, v[0], 1);
-            if (lane == 31) next = ST::ldu(Pr + dr + j * W);
+            if (lane == 31) next = in_bounds((unsigned long long)(pr + dr), NP, BS_TILE_PULL) ? ST::ldu(Pr + dr + j * W) : R(0);
             d[j][0] = v[1];
             d[j][1] = next;
         }
@@ -102,21 +105,27 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
                 continue;
             }
             if (m == LBM_OUTLET) {  // zero-gradient: e_x = -1 populations come from the own column
-                dk[3] = ST::ldu(A + pop_index(true, N, 3, (size_t)y * nx + x));
-                dk[6] = ST::ldu(A + pop_index(true, N, 6, (size_t)yp * nx + x));
-                dk[7] = ST::ldu(A + pop_index(true, N, 7, (size_t)ym * nx + x));
+                const size_t i3 = pop_index(true, N, 3, (size_t)y * nx + x);
+                const size_t i6 = pop_index(true, N, 6, (size_t)yp * nx + x);
+                const size_t i7 = pop_index(true, N, 7, (size_t)ym * nx + x);
+                dk[3] = in_bounds(i3, NP, BS_TILE_PULL) ? ST::ldu(A + i3) : R(0);
+                dk[6] = in_bounds(i6, NP, BS_TILE_PULL) ? ST::ldu(A + i6) : R(0);
+                dk[7] = in_bounds(i7, NP, BS_TILE_PULL) ? ST::ldu(A + i7) : R(0);
             }
             if (f & (0xFFu << (FL_DIR_SHIFT + 1))) {  // some pull source is solid: bounce back
 #pragma unroll
                 for (int j = 1; j < 9; ++j) {
                     if (f & (1u << (FL_DIR_SHIFT + j))) {
-                        R v = ST::ldu(A + pop_index(true, N, INV(j), c));
+                        const size_t ib = pop_index(true, N, INV(j), c);
+                        R v = in_bounds(ib, NP, BS_TILE_PULL) ? ST::ldu(A + ib) : R(0);
                         if (f & FL_MOVING) {
                             int sx = x - EX(j);
                             if (m == LBM_OUTLET && EX(j) == -1) sx = x;
                             sx = sx < 0 ? nx - 1 : (sx >= nx ? 0 : sx);
                             const int sy = EY(j) == 1 ? ym : (EY(j) == -1 ? yp : y);
-                            const lbm_lattice_info si = info[(size_t)sy * nx + sx];
+                            const size_t is = (size_t)sy * nx + sx;
+                            lbm_lattice_info si = {0, 0, 0.0f, 0.0f};
+                            if (in_bounds(is, NC, BS_TILE_INFO)) si = info[is];
                             const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
                             if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j) * R(ST::UNIT), uw));
                         }
@@ -134,12 +143,15 @@ __device__ __forceinline__ void phys_tile_update(const typename ST::T* __restric
     if (SR) {
         const uint32_t q = sr_hash(c0 ^ seed);
 #pragma unroll
-        for (int j = 0; j < 9; ++j) Vec2<ST>::st_sr(Q0 + j * W, d[j], q * sr_mul(2 * j), q * sr_mul(2 * j + 1));
+        for (int j = 0; j < 9; ++j)
+            if (in_bounds(o0 + (unsigned long long)(j * W) + 1ull, NP, BS_TILE_STORE))
+                Vec2<ST>::st_sr(Q0 + j * W, d[j], q * sr_mul(2 * j), q * sr_mul(2 * j + 1));
     } else {
 #pragma unroll
-        for (int j = 0; j < 9; ++j) Vec2<ST>::st(Q0 + j * W, d[j]);
+        for (int j = 0; j < 9; ++j)
+            if (in_bounds(o0 + (unsigned long long)(j * W) + 1ull, NP, BS_TILE_STORE)) Vec2<ST>::st(Q0 + j * W, d[j]);
     }
-    if (MACRO) {
+    if (MACRO && in_bounds(2ull * N + c0 + 1ull, NM, BS_TILE_MACRO)) {
         *reinterpret_cast<float2*>(macro + c0) = make_float2(mr[0], mr[1]);
         *reinterpret_cast<float2*>(macro + N + c0) = make_float2(mu[0], mu[1]);
         *reinterpret_cast<float2*>(macro + 2 * N + c0) = make_float2(mv[0], mv[1]);

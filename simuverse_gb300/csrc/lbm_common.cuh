@@ -12,6 +12,7 @@
 #include <stdint.h>
 
 #include "../../include/lbm.h"
+#include "lbm_internal.h"
 
 namespace lbm {
 
@@ -64,6 +65,49 @@ constexpr int POP_TILE = 64;
 __host__ __device__ __forceinline__ size_t pop_index(bool tiled, size_t N, int j, size_t c) {
     return tiled ? (c / POP_TILE) * (9 * POP_TILE) + (size_t)j * POP_TILE + (c % POP_TILE) : (size_t)j * N + c;
 }
+
+// ---- bounds-checked builds (-DLBM_BOUNDS_CHECK) ------------------------------------
+// A bounds-checked build of the library compares every population, flag and info index of
+// the step kernels with the extent of its buffer before the access.  An index outside it is
+// counted in g_bounds together with the first offending index, its extent and the access
+// site; the access is skipped (a load gives 0): nothing traps and the context stays usable.
+// lbm_bounds_report reads and clears the records.  In normal builds in_bounds is the constant
+// true and the checks compile away.
+enum BoundsSite : int {
+    BS_REF_FLAGS = 1, BS_REF_PULL, BS_REF_INFO, BS_REF_STORE, BS_REF_WALL, BS_REF_MACRO,
+    BS_CELL_FLAGS = 11, BS_CELL_PULL, BS_CELL_INFO, BS_CELL_STORE, BS_CELL_MACRO,
+    BS_TILE_FLAGS = 21, BS_TILE_PULL, BS_TILE_INFO, BS_TILE_STORE, BS_TILE_MACRO,
+    BS_BULK_COPY = 31, BS_BULK_PULL, BS_BULK_INFO, BS_BULK_STORE, BS_BULK_MACRO,
+    BS_SELFTEST = 99
+};
+#ifdef LBM_BOUNDS_CHECK
+static __device__ BoundsRecord g_bounds;  // one per translation unit
+#endif
+__device__ __forceinline__ bool in_bounds(unsigned long long idx, unsigned long long limit, int site) {
+#ifdef LBM_BOUNDS_CHECK
+    if (idx < limit) return true;
+    if (atomicAdd(&g_bounds.count, 1ull) == 0ull) {
+        g_bounds.index = idx;
+        g_bounds.limit = limit;
+        g_bounds.site = site;
+    }
+    return false;
+#else
+    (void)idx;
+    (void)limit;
+    (void)site;
+    return true;
+#endif
+}
+#ifdef LBM_BOUNDS_CHECK
+// the records of the calling translation unit on the current device, cleared after reading
+static inline cudaError_t bounds_take_local(BoundsRecord* out) {
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_bounds, sizeof(BoundsRecord));
+    if (e != cudaSuccess) return e;
+    const BoundsRecord zero = {0, 0, 0, 0, 0};
+    return cudaMemcpyToSymbol(g_bounds, &zero, sizeof(BoundsRecord));
+}
+#endif
 
 // round-to-nearest add and multiply that the compiler may not contract into an FMA
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }

@@ -89,6 +89,23 @@ struct PerDevice {
     }
 };
 
+// bounds-checked builds (LBM_BOUNDS_CHECK, see in_bounds in lbm_common.cuh): the number of
+// out-of-range indices and the first one's index, extent and access site.  Each translation
+// unit with step kernels keeps its own record on every device; bounds_take_* reads and
+// clears it on the current device (lbm_bounds_report adds them up).
+struct BoundsRecord {
+    unsigned long long count, index, limit;
+    int site, pad;
+};
+#ifdef LBM_BOUNDS_CHECK
+cudaError_t bounds_take_kernels(BoundsRecord* out);  // lbm_kernels.cu: k_ref_step, k_phys_step
+cudaError_t bounds_take_vec(BoundsRecord* out);      // lbm_step_vec.cu: k_phys_step_tiled
+cudaError_t bounds_take_bulk(BoundsRecord* out);     // lbm_step_bulk.cu: k_phys_step_bulk
+cudaError_t bounds_take_batch(BoundsRecord* out);    // lbm_batch.cu: the batched one-cell update
+// one thread evaluates one index equal to its extent (no memory access): the record must show it
+cudaError_t bounds_selftest(cudaStream_t s);
+#endif
+
 constexpr int TPB = 128;          // threads per block along x for the step kernels
 constexpr int RED_BLOCKS = 1216;  // 8 x 152 SMs; fixed so FP64 sums have a fixed order
 constexpr int RED_TPB = 256;

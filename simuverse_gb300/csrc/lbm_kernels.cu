@@ -227,13 +227,18 @@ __global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref
     if (x >= nx) return;
     const IDX N = (IDX)nx * (IDX)ny;
     const IDX c = (IDX)y * (IDX)nx + (IDX)x;
-    const unsigned fl = flags[c];
+    // extents for the bounds-checked build: cells, population elements, macro elements
+    const unsigned long long NC = (unsigned long long)N, NP = 9ull * NC, NM = 3ull * NC;
+    const unsigned fl = in_bounds(c, NC, BS_REF_FLAGS) ? flags[c] : 0u;
     const int m = (int)(fl & FL_MAT_MASK);
     if (is_solid(m)) {  // collide_stream.wgsl:34-38
-        if (MACRO) { macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f; }
+        if (MACRO && in_bounds(c + 2 * N, NM, BS_REF_MACRO)) {
+            macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f;
+        }
 #pragma unroll
         for (int k = 0; k < 9; ++k)
-            if (fl & (1u << (FL_DIR_SHIFT + k))) B[c + (IDX)k * N] = 0.0f;
+            if ((fl & (1u << (FL_DIR_SHIFT + k))) && in_bounds(c + (IDX)k * N, NP, BS_REF_STORE))
+                B[c + (IDX)k * N] = 0.0f;
         return;
     }
     // warp-uniform: no cell of the (active part of the) warp pushes into a wall slot or forces
@@ -247,7 +252,8 @@ __global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref
     for (int j = 0; j < 9; ++j) {  // source uv - e(j), wrapped
         const int sx = EX(j) == 1 ? xm : (EX(j) == -1 ? xp : x);
         const IDX row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        f[j] = __ldg(A + (row + (IDX)sx + (IDX)j * N));
+        const IDX i = row + (IDX)sx + (IDX)j * N;
+        f[j] = in_bounds(i, NP, BS_REF_PULL) ? __ldg(A + i) : 0.0f;
     }
     // collide_stream.wgsl:40-48
     float rho = 0.0f, vx = 0.0f, vy = 0.0f, inv = 0.0f;
@@ -277,7 +283,8 @@ __global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref
         vy = __fdiv_rn(vy, rho);
     }
     float fx = 0.0f, fy = 0.0f;  // the forcing term F_j = 3 w_j (e_j . f) is 0 unless a force acts
-    if (!fast && (m == LBM_INLET || m == LBM_EXTERNAL_FORCE)) {  // collide_stream.wgsl:55-71
+    if (!fast && (m == LBM_INLET || m == LBM_EXTERNAL_FORCE) && in_bounds(c, NC, BS_REF_INFO)) {
+        // collide_stream.wgsl:55-71
         lbm_lattice_info in = info[c];
         if (in.block_iter > 0) {
             in.block_iter = in.block_iter - 1;
@@ -297,7 +304,7 @@ __global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref
             vy = __fdiv_rn(__fmul_rn(fy, 0.5f), rho);
         }
     }
-    if (MACRO) { macro[c] = rho; macro[c + N] = vx; macro[c + 2 * N] = vy; }
+    if (MACRO && in_bounds(c + 2 * N, NM, BS_REF_MACRO)) { macro[c] = rho; macro[c + N] = vx; macro[c + 2 * N] = vy; }
     float t[9];
     if constexpr (FAST) {
         // t_j = (1 - omega) f_j + omega feq_j, feq of the pair (j, k = inv j) = sym +- asy
@@ -341,11 +348,13 @@ __global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref
         }
         if (v > REF_MAX(j)) v = REF_MAX(j);  // collide_stream.wgsl:79-83
         else if (v < 0.0f) v = 0.0f;
+        const IDX own = c + (IDX)j * N;
         if (!fast && (fl & (1u << (FL_DIR_SHIFT + j)))) {
-            B[c + (IDX)(EY(j) * nx + EX(j)) + (IDX)INV(j) * N] = v;
-            B[c + (IDX)j * N] = 0.0f;
-        } else {
-            B[c + (IDX)j * N] = v;
+            const IDX wall = c + (IDX)(EY(j) * nx + EX(j)) + (IDX)INV(j) * N;
+            if (in_bounds(wall, NP, BS_REF_WALL)) B[wall] = v;
+            if (in_bounds(own, NP, BS_REF_STORE)) B[own] = 0.0f;
+        } else if (in_bounds(own, NP, BS_REF_STORE)) {
+            B[own] = v;
         }
     }
 }
@@ -816,5 +825,18 @@ cudaError_t launch_from_absolute(lbm_handle* h, const void* src, int sd, void* s
         default: return from_abs_t<StoreBF16>(h, src, sd, state, s);
     }
 }
+
+#ifdef LBM_BOUNDS_CHECK
+cudaError_t bounds_take_kernels(BoundsRecord* out) { return bounds_take_local(out); }
+
+__global__ void k_bounds_selftest() {
+    if (threadIdx.x == 0 && blockIdx.x == 0) (void)in_bounds(7ull, 7ull, BS_SELFTEST);
+}
+
+cudaError_t bounds_selftest(cudaStream_t s) {
+    k_bounds_selftest<<<1, 32, 0, s>>>();
+    return cudaGetLastError();
+}
+#endif
 
 }  // namespace lbm

@@ -184,24 +184,36 @@ __device__ __forceinline__ void bulk_issue(const typename ST::T* __restrict__ A,
     if (tid == 0) {
         const unsigned seg_bytes = (unsigned)(c1 - c0) * (unsigned)sizeof(typename ST::T);
         const int sofs = c0 - (g.x0 - L::H);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of this stage
-        mbar_arrive_expect_tx(bar, 9 * seg_bytes + (unsigned)g.tw * 2u);
+        // bounds-checked build: every copy's last element inside its buffer, else none is
+        // started and the stage's phase completes with no bytes (its contents are stale)
+        bool ok = in_bounds(r0 + (size_t)g.x0 + (size_t)g.tw - 1, N, BS_BULK_COPY);
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
             const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-            bulk_g2s(sp + j * L::ROW + sofs, A + (size_t)j * N + row + c0, seg_bytes, bar);
+            ok = in_bounds((size_t)j * N + row + (size_t)c1 - 1, 9 * N, BS_BULK_COPY) && ok;
         }
-        bulk_g2s(sfl, flags + r0 + g.x0, (unsigned)g.tw * 2u, bar);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of this stage
+        mbar_arrive_expect_tx(bar, ok ? 9 * seg_bytes + (unsigned)g.tw * 2u : 0u);
+        if (ok) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
+                bulk_g2s(sp + j * L::ROW + sofs, A + (size_t)j * N + row + c0, seg_bytes, bar);
+            }
+            bulk_g2s(sfl, flags + r0 + g.x0, (unsigned)g.tw * 2u, bar);
+        }
     }
     if (tid < 9 && g.x0 == 0) {  // x = -1 wraps to nx - 1
         const int j = tid;
         const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        sp[j * L::ROW + L::H - 1] = A[(size_t)j * N + row + (nx - 1)];
+        const size_t i = (size_t)j * N + row + (nx - 1);
+        if (in_bounds(i, 9 * N, BS_BULK_PULL)) sp[j * L::ROW + L::H - 1] = A[i];
     }
     if (tid >= 16 && tid < 25 && g.x0 + g.tw == nx) {  // x = nx wraps to 0
         const int j = tid - 16;
         const size_t row = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-        sp[j * L::ROW + L::H + g.tw] = A[(size_t)j * N + row];
+        const size_t i = (size_t)j * N + row;
+        if (in_bounds(i, 9 * N, BS_BULK_PULL)) sp[j * L::ROW + L::H + g.tw] = A[i];
     }
 }
 
@@ -311,13 +323,15 @@ __global__ void __launch_bounds__(BULK_TPB) k_phys_step_bulk(const typename ST::
 #pragma unroll
                     for (int j = 1; j < 9; ++j) {
                         if (f & (1u << (FL_DIR_SHIFT + j))) {
-                            R v = ST::ld(A + c + (size_t)INV(j) * N);
+                            const size_t ib = c + (size_t)INV(j) * N;
+                            R v = in_bounds(ib, 9 * N, BS_BULK_PULL) ? ST::ld(A + ib) : R(0);
                             if (f & FL_MOVING) {
                                 int sx = x - EX(j);
                                 if (m == LBM_OUTLET && EX(j) == -1) sx = x;
                                 sx = sx < 0 ? nx - 1 : (sx >= nx ? 0 : sx);
                                 const size_t srow = EY(j) == 1 ? rm : (EY(j) == -1 ? rp : r0);
-                                const lbm_lattice_info si = info[srow + sx];
+                                lbm_lattice_info si = {0, 0, 0.0f, 0.0f};
+                                if (in_bounds(srow + sx, N, BS_BULK_INFO)) si = info[srow + sx];
                                 const R uw = R(EX(j)) * R(si.vx) + R(EY(j)) * R(si.vy);
                                 if (uw != R(0)) v = add_rn(v, mul_rn(R(6) * PW<R>(j), uw));
                             }
@@ -332,8 +346,9 @@ __global__ void __launch_bounds__(BULK_TPB) k_phys_step_bulk(const typename ST::
             }
             const size_t cs = r0 + g.x0 + xl;
 #pragma unroll
-            for (int j = 0; j < 9; ++j) vec4_store<ST>(B + (size_t)j * N + cs, d[j]);
-            if (MACRO) {
+            for (int j = 0; j < 9; ++j)
+                if (in_bounds((size_t)j * N + cs + 3, 9 * N, BS_BULK_STORE)) vec4_store<ST>(B + (size_t)j * N + cs, d[j]);
+            if (MACRO && in_bounds(2 * N + cs + 3, 3 * N, BS_BULK_MACRO)) {
                 *reinterpret_cast<float4*>(macro + cs) =
                     make_float4((float)mr[0], (float)mr[1], (float)mr[2], (float)mr[3]);
                 *reinterpret_cast<float4*>(macro + N + cs) =
@@ -397,5 +412,9 @@ cudaError_t launch_phys_step_bulk(lbm_handle* h, bool write_macro, cudaStream_t 
         default: return write_macro ? bulk_t<StoreBF16, true>(h, s) : bulk_t<StoreBF16, false>(h, s);
     }
 }
+
+#ifdef LBM_BOUNDS_CHECK
+cudaError_t bounds_take_bulk(BoundsRecord* out) { return bounds_take_local(out); }
+#endif
 
 }  // namespace lbm

@@ -140,4 +140,8 @@ cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s
     }
 }
 
+#ifdef LBM_BOUNDS_CHECK
+cudaError_t bounds_take_vec(BoundsRecord* out) { return bounds_take_local(out); }
+#endif
+
 }  // namespace lbm
