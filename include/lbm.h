@@ -475,6 +475,16 @@ int lbm_closure_set_scales(lbm_closure* c, float s_in, float s_out);
 #define LBM_CLOSURE_PROJECT_CELL 0
 #define LBM_CLOSURE_PROJECT_DOMAIN 1
 int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t projection);
+/* inference kernel of lbm_closure_apply / lbm_closure_predict: FUSED (default) computes the
+   features and the three layers in one kernel on the tcgen05 tensor cores with the activations
+   in shared and tensor memory; LAYERS runs the feature kernel and one mma.sync kernel per
+   layer with the activations in device memory (the training path's kernels).  Both give the
+   same network within BF16 rounding of the activations. */
+#define LBM_CLOSURE_KERNEL_FUSED 0
+#define LBM_CLOSURE_KERNEL_LAYERS 1
+int lbm_closure_set_kernel(lbm_closure* c, int32_t kernel);
+/* synchronises; LBM_ERR_TIMEOUT if the fused kernel gave up on a bounded wait since creation */
+int lbm_closure_status(lbm_closure* c);
 int lbm_closure_get_params(lbm_closure* c, float* out);
 int lbm_closure_set_params(lbm_closure* c, const float* in);
 /* coarse = block average over factor x factor cells of the fine lattice's density and

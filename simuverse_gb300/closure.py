@@ -59,6 +59,18 @@ class Closure:
                                                  self.PROJECTIONS[projection]))
         self.inputs, self.target, self.projection = inputs, target, projection
 
+    KERNELS = {"fused": 0, "layers": 1}
+
+    def set_kernel(self, kernel: str = "fused"):
+        """Inference kernel of apply / predict: 'fused' (one tcgen05 kernel, activations on chip)
+        or 'layers' (feature kernel + one mma.sync kernel per layer)."""
+        nat.check(self._lib.lbm_closure_set_kernel(self._h, self.KERNELS[kernel]))
+        self.kernel = kernel
+
+    def status(self):
+        """Synchronises; raises LbmError if the fused kernel gave up on a bounded wait."""
+        nat.check(self._lib.lbm_closure_status(self._h))
+
     @property
     def params(self) -> np.ndarray:
         out = np.empty(self.nparams, np.float32)

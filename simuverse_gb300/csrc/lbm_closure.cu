@@ -366,6 +366,8 @@ __global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* __restrict__ 
     }
 }
 
+#include "lbm_closure_tc.cuh"
+
 }  // namespace closure
 }  // namespace lbm
 
@@ -381,6 +383,8 @@ struct lbm_closure {
     int inputs = LBM_CLOSURE_INPUT_NEQ;
     int target = LBM_CLOSURE_TARGET_POPULATIONS;
     int projection = LBM_CLOSURE_PROJECT_CELL;
+    int kernel = LBM_CLOSURE_KERNEL_FUSED;  // inference: one tcgen05 kernel, or the three layer kernels
+    int* d_status = nullptr;                // LBM_ERR_TIMEOUT from a bounded wait of the fused kernel
     double* dmeans = nullptr;  // reduction partials (RED_BLOCKS x 3) and the 3 field means
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -572,6 +576,8 @@ int lbm_closure_create(int32_t nx, int32_t ny, uint64_t seed, lbm_closure** out)
     if (e == cudaSuccess) e = dalloc(&c->dmeans, (size_t)lbm::RED_BLOCKS * 3 + 3);
     if (e == cudaSuccess) e = dalloc(&c->dloss, 8);
     if (e == cudaSuccess) e = dalloc(&c->dwpart, (size_t)cl::DW_BLOCKS * (9 * 32 * 32 + 32));
+    if (e == cudaSuccess) e = dalloc(&c->d_status, 1);
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
         lbm_closure_destroy(c);
         return cfail(LBM_ERR_CUDA, "closure allocation: %s", cudaGetErrorString(e));
@@ -612,7 +618,7 @@ int lbm_closure_destroy(lbm_closure* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->p,  c->g,  c->m,   c->v,   c->mask, c->wf1, c->wf2, c->wf3, c->wb3, c->wb2, c->x0,
                     c->x1, c->x2, c->y,   c->dsx, c->dst,  c->bx0, c->bt,  c->bx1, c->bx2, c->bg3, c->bg2,
-                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans};
+                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans, c->d_status};
     for (void* b : bufs) cudaFree(b);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -700,11 +706,38 @@ int correction(lbm_closure* c, lbm_handle* h, float* out, int accumulate) {
     cudaStream_t keep = c->stream;
     c->stream = s;  // run on the lattice's stream
     const dim3 g1((unsigned)((c->nx + 127) / 128), (unsigned)c->ny);
-    cl::k_features<<<g1, 128, 0, s>>>((const float*)h->buf[h->cur], c->nx, c->ny, 0, 0, c->ny, c->nx, c->s_in,
-                                      c->inputs, c->x0);
-    cudaError_t e = cudaGetLastError();
-    int r = e == cudaSuccess ? forward<true>(c, c->x0, c->x1, c->x2, c->y, 1, c->ny, c->nx)
+    cudaError_t e = cudaSuccess;
+    int r = LBM_OK;
+    if (c->kernel == LBM_CLOSURE_KERNEL_FUSED) {
+        // features and the three layers in one tcgen05 kernel (its shared-memory attribute is
+        // set per device)
+        static lbm::PerDevice<bool> attr;
+        bool done = false;
+        e = attr.get(
+            c->device,
+            [](bool& v) {
+                v = true;
+                return cudaFuncSetAttribute(cl::tc::k_closure_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            cl::tc::SMEM_BYTES);
+            },
+            &done);
+        if (e == cudaSuccess) {
+            const dim3 grid((unsigned)((c->nx + cl::tc::OUT_W - 1) / cl::tc::OUT_W),
+                            (unsigned)((c->ny + cl::tc::TC_ROWS - 1) / cl::tc::TC_ROWS));
+            cl::tc::k_closure_fused<<<grid, cl::tc::TC_THREADS, cl::tc::SMEM_BYTES, s>>>(
+                (const float*)h->buf[h->cur], c->nx, c->ny, c->s_in, c->inputs, c->wf1, c->wf2, c->wf3, c->p + cl::OB1,
+                c->p + cl::OB2, c->p + cl::OB3, c->y, c->d_status);
+            e = cudaGetLastError();
+            ++c->launches;
+        }
+        if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "fused closure kernel: %s", cudaGetErrorString(e));
+    } else {
+        cl::k_features<<<g1, 128, 0, s>>>((const float*)h->buf[h->cur], c->nx, c->ny, 0, 0, c->ny, c->nx, c->s_in,
+                                          c->inputs, c->x0);
+        e = cudaGetLastError();
+        r = e == cudaSuccess ? forward<true>(c, c->x0, c->x1, c->x2, c->y, 1, c->ny, c->nx)
                              : cfail(LBM_ERR_CUDA, "features: %s", cudaGetErrorString(e));
+    }
     const double* means = nullptr;
     if (r == LBM_OK && c->projection == LBM_CLOSURE_PROJECT_DOMAIN) {
         const size_t N = (size_t)c->nx * c->ny;
@@ -735,8 +768,27 @@ int lbm_closure_apply(lbm_closure* c, lbm_handle* h) {
     C_TRY(check_coarse(c, h));
     C_CK(cudaSetDevice(c->device));
     const int r = correction(c, h, (float*)h->buf[h->cur], 1);
-    h->launches += c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 7 : 5;
+    const int layers = c->kernel == LBM_CLOSURE_KERNEL_FUSED ? 1 : 4;  // kernels before the correction
+    h->launches += layers + (c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 3 : 1);
     return r;
+}
+
+int lbm_closure_set_kernel(lbm_closure* c, int32_t kernel) {
+    C_TRY(check_closure(c));
+    if (kernel != LBM_CLOSURE_KERNEL_FUSED && kernel != LBM_CLOSURE_KERNEL_LAYERS)
+        return cfail(LBM_ERR_ARG, "unknown closure kernel %d", kernel);
+    c->kernel = kernel;
+    return LBM_OK;
+}
+
+int lbm_closure_status(lbm_closure* c) {
+    C_TRY(check_closure(c));
+    C_CK(cudaSetDevice(c->device));
+    C_CK(cudaDeviceSynchronize());
+    int st = 0;
+    C_CK(cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st != 0) return cfail(st, "the fused closure kernel gave up on a bounded wait");
+    return LBM_OK;
 }
 
 int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t batch) {

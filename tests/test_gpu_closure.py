@@ -250,3 +250,37 @@ def test_fine_lattice_is_the_fallback(gpu):
     for s_ in (fine, plain):
         s_.close()
 
+
+
+@pytest.mark.parametrize("size", [(256, 80), (16, 4), (1024, 1024)], ids=["partial-strips", "tiny-wrapped", "c5-coarse"])
+@pytest.mark.parametrize("form", FORMS, ids=["-".join(f) for f in FORMS])
+def test_fused_tcgen05_kernel_matches_layer_kernels(gpu, size, form):
+    """The fused inference kernel (features and three layers on the tcgen05 tensor cores, the
+    activations in shared and tensor memory) against the three mma.sync layer kernels on the
+    same parameters: strips of 124 columns and 32 rows that end inside the lattice, a lattice
+    smaller than one strip (every coordinate wraps), and the 1024^2 coarse lattice of the
+    closure study.  Both round the activations to BF16; they differ only in the order of the
+    FP32 sums, so the corrections agree to 2e-2 of their largest value (mean 2e-3)."""
+    inputs, target, projection = form
+    nx, ny = size
+    rng = np.random.default_rng(7)
+    c = Closure(nx, ny, seed=2, s_in=3000.0 if inputs == "neq" else 20.0, s_out=500.0, inputs=inputs, target=target,
+                projection=projection)
+    c.params = _random_params(c, rng)
+    sim = _turbulent_sim(nx, ny, 11, steps=10)
+    c.set_kernel("layers")
+    ref_delta = c.predict(sim)
+    c.set_kernel("fused")
+    got = c.predict(sim)
+    c.status()
+    scale = np.max(np.abs(ref_delta))
+    assert scale > 0
+    err = np.abs(got - ref_delta)
+    assert np.max(err) / scale < 2e-2, np.max(err) / scale
+    assert np.mean(err) / scale < 2e-3, np.mean(err) / scale
+    # apply() through the fused kernel conserves what the projection conserves
+    m0 = sim.conservation()
+    c.apply(sim)
+    m1 = sim.conservation()
+    assert abs(m1[0] - m0[0]) <= 1e-9 * m0[0]
+    assert abs(m1[1] - m0[1]) <= 1e-9 * m0[0] and abs(m1[2] - m0[2]) <= 1e-9 * m0[0]
