@@ -721,16 +721,26 @@ int correction(lbm_closure* c, lbm_handle* h, float* out, int accumulate) {
                                             cl::tc::SMEM_BYTES);
             },
             &done);
+        // applying a per-cell projected correction needs no field reduction: the kernel adds it
+        // itself and writes the corrected state into the lattice's other buffer
+        const bool in_kernel = accumulate && out == (float*)h->buf[h->cur] && c->projection == LBM_CLOSURE_PROJECT_CELL;
         if (e == cudaSuccess) {
             const dim3 grid((unsigned)((c->nx + cl::tc::OUT_W - 1) / cl::tc::OUT_W),
                             (unsigned)((c->ny + cl::tc::TC_ROWS - 1) / cl::tc::TC_ROWS));
             cl::tc::k_closure_fused<<<grid, cl::tc::TC_THREADS, cl::tc::SMEM_BYTES, s>>>(
                 (const float*)h->buf[h->cur], c->nx, c->ny, c->s_in, c->inputs, c->wf1, c->wf2, c->wf3, c->p + cl::OB1,
-                c->p + cl::OB2, c->p + cl::OB3, c->y, c->d_status);
+                c->p + cl::OB2, c->p + cl::OB3, c->y, in_kernel ? (float*)h->buf[h->cur ^ 1] : nullptr,
+                1.0f / c->s_out, c->d_status);
             e = cudaGetLastError();
             ++c->launches;
         }
-        if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "fused closure kernel: %s", cudaGetErrorString(e));
+        if (e != cudaSuccess) {
+            r = cfail(LBM_ERR_CUDA, "fused closure kernel: %s", cudaGetErrorString(e));
+        } else if (in_kernel) {
+            h->cur ^= 1;  // the corrected state is the one the next step reads
+            c->stream = keep;
+            return LBM_OK;
+        }
     } else {
         cl::k_features<<<g1, 128, 0, s>>>((const float*)h->buf[h->cur], c->nx, c->ny, 0, 0, c->ny, c->nx, c->s_in,
                                           c->inputs, c->x0);
@@ -768,8 +778,10 @@ int lbm_closure_apply(lbm_closure* c, lbm_handle* h) {
     C_TRY(check_coarse(c, h));
     C_CK(cudaSetDevice(c->device));
     const int r = correction(c, h, (float*)h->buf[h->cur], 1);
-    const int layers = c->kernel == LBM_CLOSURE_KERNEL_FUSED ? 1 : 4;  // kernels before the correction
-    h->launches += layers + (c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 3 : 1);
+    if (c->kernel == LBM_CLOSURE_KERNEL_FUSED)  // one kernel, plus the field means and the apply pass
+        h->launches += c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 4 : 1;
+    else
+        h->launches += 4 + (c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 3 : 1);
     return r;
 }
 

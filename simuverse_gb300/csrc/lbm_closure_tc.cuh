@@ -6,32 +6,40 @@
 // the lattice's populations computed on the fly: the activations never leave shared memory and
 // tensor memory.
 //
-// Tiling.  A CTA owns a strip of OUT_W = 124 output columns and TC_ROWS = 32 output rows.  It walks
-// down the rows with three ring buffers of three rows each in shared memory: input features
-// (16 channels), layer-1 and layer-2 activations (32 channels, BF16).  Every ring row holds
-// POS = 130 positions, position p being column x0 - 3 + p (wrapped): one MMA row block of 128
-// positions plus the two positions its 3-wide stencil reads beyond them.  Output position p of a
-// layer is MMA row p - 1, its A operand for tap (dy, dx) the 128 positions starting at dx of ring
-// row (r - 1 + dy); each layer loses one position per side, so layer 3 is valid at positions
-// 3..126 = the strip's 124 columns.  Per row: layer 1 (9 MMAs of M128 N32 K16), layer 2 (18 MMAs
-// M128 N32 K16), layer 3 (18 MMAs M128 N16 K16).
+// Tiling.  A CTA owns a strip of OUT_W = 124 output columns and TC_ROWS = 32 output rows and walks
+// down its rows.  A row of every activation -- input features (16 channels), layer-1 and layer-2
+// outputs (32 channels, BF16) -- holds POS = 130 positions, position p being column x0 - 3 + p
+// (wrapped): one MMA row block of 128 positions plus the two positions a 3-wide stencil reads
+// beyond them.  Output position p of a layer is MMA row p - 1; each layer loses one position per
+// side, so layer 3 is valid at positions 3..126 = the strip's 124 columns.
+//
+// Rows stacked along N.  A layer reads each of its input rows r once: for each column shift dx
+// (and 16-channel chunk) one MMA multiplies the 128 positions starting at dx by the weights of
+// all three row taps dy side by side (N = 3 x cout), contributing to output rows r + 1 - dy.
+// Output row o accumulates in tensor-memory slot o % 3 (cout columns each); the weights are
+// stored in the row-tap order [2, 1, 0, 2, 1], so the order a row r needs -- slot k receives
+// tap (r + 1 - k) mod 3 -- is three consecutive blocks starting at (1 - r) mod 3.  A row is
+// complete after its last contributing input row; the epilogue reads it, zeroes the slot with
+// tcgen05.st for row o + 3, and writes the BF16 activations (bias, ReLU) to the next layer's
+// input, double-buffered in shared memory.  Per input row: layer 1 3 MMAs of M128 N96 K16,
+// layer 2 6 of M128 N96 K16, layer 3 6 of M128 N48 K16.
 //
 // Operands.  Shared-memory matrices in the canonical K-major layout without swizzle: core
-// matrices of 8 rows x 16 bytes (8 BF16 channels); a ring row stores its channel groups as planes
-// of POS x 16 bytes, so the descriptor's leading (K-direction) byte offset is POS * 16 and its
-// stride (8-row) offset 128; weights [tap][channel group][cout][8] with leading offset cout * 16.
-// The descriptor encoding and the accumulator lane layout (thread t of the warpgroup reads TMEM
-// lane t = MMA row t with tcgen05.ld 32x32b) were checked against a host product before use.
+// matrices of 8 rows x 16 bytes (8 BF16 channels); an activation row stores its channel groups as
+// planes of POS x 16 bytes, so the descriptor's leading (K-direction) byte offset is POS * 16 and
+// its stride (8-row) offset 128; weights [dx][channel group][row-tap block 5][cout][8] with leading
+// offset 5 * cout * 16.  The descriptor encoding and the accumulator lane layout (warp w reads
+// TMEM lanes 32 (w % 4) .. + 31 = MMA rows with tcgen05.ld 32x32b) were checked against a host
+// product before use.  The CTA's two warpgroups split every epilogue by accumulator columns.
 //
-// Schedule.  Step a issues one batch of MMAs: layer-1 row a - 1, layer-2 row a - 3 and layer-3
-// row a - 5, which depend only on rows finished in earlier steps, committed to one mbarrier.
-// While the batch runs the block loads the populations of the next input row; after it, the
-// epilogues (bias, ReLU, BF16) write the new layer rows over the ring rows that the batch was the
-// last to read, the output row of layer 3 to global memory, and the next row's features.
-// Generic shared-memory writes are fenced to the async proxy before the next batch.  Thread 0
-// waits on the mbarrier with a 1 s limit and the block follows its outcome; a timed-out wait
-// records LBM_ERR_TIMEOUT, waits (bounded) for the MMAs in flight, frees the tensor memory and
-// leaves.
+// Schedule.  Step a issues one batch: layer 1 on input row a, layer 2 on layer-1 row a - 2,
+// layer 3 on layer-2 row a - 4 (rows finished in earlier steps), committed to one mbarrier.
+// While the batch runs the block loads the populations of input row a + 1; after it, the
+// epilogues finish layer-1 row a - 1, layer-2 row a - 3 and layer-3 row a - 5 (the output row,
+// to global memory) and store the features of row a + 1.  Generic shared-memory writes are fenced
+// to the async proxy before the next batch.  Thread 0 waits on the mbarrier with a 1 s limit
+// and the block follows its outcome; a timed-out wait records LBM_ERR_TIMEOUT, waits (bounded)
+// for the MMAs in flight, frees the tensor memory and leaves.
 #pragma once
 
 namespace tc {
@@ -39,21 +47,23 @@ namespace tc {
 constexpr int POS = 130;           // ring-row positions: columns x0 - 3 .. x0 + 126
 constexpr int OUT_W = 124;         // output columns per strip (positions 3 .. 126)
 constexpr int TC_ROWS = 32;        // output rows per CTA
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;  // two warpgroups: each epilogue is split between them by columns
 constexpr int PLANE = POS * 16;    // bytes of one 8-channel group of a ring row
 constexpr int IN_ROW = 2 * PLANE;  // 16 input channels
 constexpr int H_ROW = 4 * PLANE;   // 32 hidden channels
-constexpr int OFF_IN = 0;
-constexpr int OFF_L1 = OFF_IN + 3 * IN_ROW;
-constexpr int OFF_L2 = OFF_L1 + 3 * H_ROW;
-constexpr int OFF_W1 = OFF_L2 + 3 * H_ROW;
-constexpr int OFF_W2 = OFF_W1 + 9 * 2 * 32 * 16;
-constexpr int OFF_W3 = OFF_W2 + 9 * 4 * 32 * 16;
-constexpr int OFF_BIAS = OFF_W3 + 9 * 4 * 16 * 16;
+constexpr int OFF_IN = 0;                        // input rows, double-buffered
+constexpr int OFF_L1 = OFF_IN + 2 * IN_ROW;      // layer-1 rows, double-buffered
+constexpr int OFF_L2 = OFF_L1 + 2 * H_ROW;       // layer-2 rows, double-buffered
+constexpr int OFF_W1 = OFF_L2 + 2 * H_ROW;       // [dx 3][group 2][block 5][cout 32] x 16 B
+constexpr int OFF_W2 = OFF_W1 + 3 * 2 * 5 * 32 * 16;  // [3][4][5][32]
+constexpr int OFF_W3 = OFF_W2 + 3 * 4 * 5 * 32 * 16;  // [3][4][5][16]
+constexpr int OFF_BIAS = OFF_W3 + 3 * 4 * 5 * 16 * 16;
 constexpr int OFF_BAR = OFF_BIAS + 80 * 4;
 constexpr int OFF_TSLOT = OFF_BAR + 8;
 constexpr int SMEM_BYTES = ((OFF_TSLOT + 4 + 127) / 128) * 128;
-constexpr int TMEM_COLS = 128;  // layer 1: columns 0-31, layer 2: 32-63, layer 3: 64-79
+// accumulators: layer 1 columns 0-95 (3 row slots of 32), layer 2 96-191, layer 3 192-239
+constexpr int TM_L1 = 0, TM_L2 = 96, TM_L3 = 192;
+constexpr int TMEM_COLS = 256;
 constexpr unsigned long long WAIT_NS = 1000000000ull;
 
 static_assert(OFF_L1 % 16 == 0 && OFF_L2 % 16 == 0 && OFF_W1 % 16 == 0 && OFF_W2 % 16 == 0 && OFF_W3 % 16 == 0,
@@ -111,21 +121,7 @@ __device__ __forceinline__ bool bar_wait_bounded(unsigned bar, unsigned parity) 
     return true;
 }
 
-// 32 / 16 consecutive accumulator columns of this thread's lane
-__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
-    unsigned r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-}
+// 16 / 8 consecutive accumulator columns of this thread's lane
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
     unsigned r[16];
     asm volatile(
@@ -138,46 +134,77 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// 32 hidden activations (bias + ReLU, BF16) into ring row `row` at position p: 4 channel groups
-__device__ __forceinline__ void store_hidden(unsigned char* row, int p, const float (&v)[32], const float* bias) {
+// zeros into 16 / 8 consecutive accumulator columns of this thread's lane
+__device__ __forceinline__ void tmem_zero16(unsigned taddr) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(
+                     taddr),
+                 "r"(0u)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_zero8(unsigned taddr) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(0u)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld8(unsigned taddr, float (&v)[8]) {
+    unsigned r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int g = 0; g < 4; ++g) {
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// 16 hidden activations, channels 16 h .. 16 h + 15 (bias + ReLU, BF16), into ring row `row` at
+// position p: channel groups 2 h and 2 h + 1
+__device__ __forceinline__ void store_hidden16(unsigned char* row, int p, int h, const float (&v16)[16],
+                                               const float* bias) {
+#pragma unroll
+    for (int gg = 0; gg < 2; ++gg) {
+        const int g = 2 * h + gg;
+        const float* vv = v16 + 8 * gg;
+        const float* bb = bias + 8 * g;
         uint4 q;
-        q.x = pack_bf16x2(fmaxf(v[8 * g + 0] + bias[8 * g + 0], 0.0f), fmaxf(v[8 * g + 1] + bias[8 * g + 1], 0.0f));
-        q.y = pack_bf16x2(fmaxf(v[8 * g + 2] + bias[8 * g + 2], 0.0f), fmaxf(v[8 * g + 3] + bias[8 * g + 3], 0.0f));
-        q.z = pack_bf16x2(fmaxf(v[8 * g + 4] + bias[8 * g + 4], 0.0f), fmaxf(v[8 * g + 5] + bias[8 * g + 5], 0.0f));
-        q.w = pack_bf16x2(fmaxf(v[8 * g + 6] + bias[8 * g + 6], 0.0f), fmaxf(v[8 * g + 7] + bias[8 * g + 7], 0.0f));
+        q.x = pack_bf16x2(fmaxf(vv[0] + bb[0], 0.0f), fmaxf(vv[1] + bb[1], 0.0f));
+        q.y = pack_bf16x2(fmaxf(vv[2] + bb[2], 0.0f), fmaxf(vv[3] + bb[3], 0.0f));
+        q.z = pack_bf16x2(fmaxf(vv[4] + bb[4], 0.0f), fmaxf(vv[5] + bb[5], 0.0f));
+        q.w = pack_bf16x2(fmaxf(vv[6] + bb[6], 0.0f), fmaxf(vv[7] + bb[7], 0.0f));
         *reinterpret_cast<uint4*>(row + g * PLANE + p * 16) = q;
     }
 }
 
-// one layer row: 9 taps x KC channel chunks of 16; A from ring rows (r - 1 + dy), B from the
-// layer's weights [tap][group][cout][8] (cout rows of 16 bytes per group)
+// the MMAs of one input row r of a layer: per column shift dx and 16-channel chunk kc, the 128
+// positions starting at dx times the three row taps' weights side by side (N = 3 x COUT), into
+// the three accumulator slots; the weight blocks start at (1 - r) mod 3 of the stored order
 template <int KC, int COUT>
-__device__ __forceinline__ void issue_layer(unsigned dtmem, unsigned ring, int ring_row_bytes, int r, unsigned wts) {
-    constexpr uint32_t ID = idesc_bf16(128, COUT);
+__device__ __forceinline__ void issue_row(unsigned dtmem, unsigned in_row, int r, unsigned wts) {
+    constexpr uint32_t ID = idesc_bf16(128, 3 * COUT);
+    constexpr unsigned LBO_W = 5 * COUT * 16;
+    const int s0 = ((1 - r) % 3 + 3) % 3;
 #pragma unroll
-    for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3, dx = tap % 3;
-        const unsigned arow = ring + (unsigned)(((r - 1 + dy) % 3) * ring_row_bytes) + (unsigned)(dx * 16);
+    for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
         for (int kc = 0; kc < KC; ++kc) {
-            const uint64_t a = sdesc(arow + (unsigned)(2 * kc * PLANE), PLANE, 128);
-            const uint64_t b = sdesc(wts + (unsigned)((tap * 2 * KC + 2 * kc) * COUT * 16), COUT * 16, 128);
-            mma(dtmem, a, b, ID, (tap | kc) != 0 ? 1u : 0u);
+            const uint64_t a = sdesc(in_row + (unsigned)(dx * 16 + 2 * kc * PLANE), PLANE, 128);
+            const uint64_t b = sdesc(wts + (unsigned)(((dx * 2 * KC + 2 * kc) * 5 + s0) * COUT * 16), LBO_W, 128);
+            mma(dtmem, a, b, ID, 1u);
         }
-    }
 }
 
 // Inference of the whole network on an nx x ny periodic lattice.  d: the lattice's populations
 // (FP32 deviations, 9 planes); w1 [9][32][16], w2 [9][32][32], w3 [9][16][32] BF16 (tap, cout,
-// cin); b1 [32], b2 [32], b3 [16] FP32; y: [nx * ny][16] FP32 outputs (9 used).
+// cin); b1 [32], b2 [32], b3 [16] FP32.  With d_next == nullptr the outputs go to y ([nx * ny][16]
+// FP32, 9 used); otherwise the correction is applied here: d_next = d + inv_s_out * P(y) cell by
+// cell (P removes a cell's density and momentum), d_next being a buffer other than d (the CTAs
+// read each other's halo rows of d).
 // Grid (ceil(nx / OUT_W), ceil(ny / TC_ROWS)), TC_THREADS threads, SMEM_BYTES dynamic shared memory.
 __global__ void __launch_bounds__(TC_THREADS, 2)
     k_closure_fused(const float* __restrict__ d, int nx, int ny, float s_in, int inputs,
                     const __nv_bfloat16* __restrict__ w1, const __nv_bfloat16* __restrict__ w2,
                     const __nv_bfloat16* __restrict__ w3, const float* __restrict__ b1, const float* __restrict__ b2,
-                    const float* __restrict__ b3, float* __restrict__ y, int* __restrict__ status) {
+                    const float* __restrict__ b3, float* __restrict__ y, float* __restrict__ d_next, float inv_s_out,
+                    int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -190,18 +217,22 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     const unsigned bar = su32(sm + OFF_BAR);
     unsigned* tslot = reinterpret_cast<unsigned*>(sm + OFF_TSLOT);
 
-    // rings to zero (positions no layer writes stay finite), weights to the operand layout
+    // activation rows to zero (positions no layer writes stay finite); weights to the operand
+    // layout, row-tap block i holding tap dy = (2 - i) mod 3
     for (int i = tid; i < OFF_W1 / 16; i += TC_THREADS) reinterpret_cast<uint4*>(sm)[i] = make_uint4(0, 0, 0, 0);
-    for (int i = tid; i < 9 * 2 * 32; i += TC_THREADS) {  // (tap, group, cout)
-        const int n = i % 32, g = (i / 32) % 2, t = i / 64;
+    for (int i = tid; i < 3 * 2 * 5 * 32; i += TC_THREADS) {  // (dx, group, block, cout)
+        const int n = i % 32, blk = (i / 32) % 5, g = (i / 160) % 2, dx = i / 320;
+        const int t = 3 * ((2 - blk + 3) % 3) + dx;
         *reinterpret_cast<uint4*>(sm + OFF_W1 + i * 16) = *reinterpret_cast<const uint4*>(w1 + (t * 32 + n) * 16 + g * 8);
     }
-    for (int i = tid; i < 9 * 4 * 32; i += TC_THREADS) {
-        const int n = i % 32, g = (i / 32) % 4, t = i / 128;
+    for (int i = tid; i < 3 * 4 * 5 * 32; i += TC_THREADS) {
+        const int n = i % 32, blk = (i / 32) % 5, g = (i / 160) % 4, dx = i / 640;
+        const int t = 3 * ((2 - blk + 3) % 3) + dx;
         *reinterpret_cast<uint4*>(sm + OFF_W2 + i * 16) = *reinterpret_cast<const uint4*>(w2 + (t * 32 + n) * 32 + g * 8);
     }
-    for (int i = tid; i < 9 * 4 * 16; i += TC_THREADS) {
-        const int n = i % 16, g = (i / 16) % 4, t = i / 64;
+    for (int i = tid; i < 3 * 4 * 5 * 16; i += TC_THREADS) {
+        const int n = i % 16, blk = (i / 16) % 5, g = (i / 80) % 4, dx = i / 320;
+        const int t = 3 * ((2 - blk + 3) % 3) + dx;
         *reinterpret_cast<uint4*>(sm + OFF_W3 + i * 16) = *reinterpret_cast<const uint4*>(w3 + (t * 16 + n) * 32 + g * 8);
     }
     if (tid < 32) {
@@ -224,7 +255,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     __syncthreads();
     fence_after();
     const unsigned tmem = *tslot;
-    const unsigned lane_off = (unsigned)(warp * 32) << 16;
+    // warp w reads TMEM lanes 32 (w % 4) .. + 31 (MMA rows = positions - 1); warpgroup h = w / 4
+    // takes half of every accumulator row's columns
+    const int lane_q = warp & 3, half = warp >> 2;
+    const int mrow = lane_q * 32 + (tid & 31);  // this thread's MMA row
+    const unsigned lane_off = (unsigned)(lane_q * 32) << 16;
+    // every accumulator slot starts at zero (each warpgroup its half of the columns)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) tmem_zero16(tmem + lane_off + 32 * k + 16 * half);  // layers 1 and 2
+#pragma unroll
+    for (int k = 0; k < 3; ++k) tmem_zero8(tmem + lane_off + TM_L3 + 16 * k + 8 * half);
+    tmem_wait_st();
     unsigned parity = 0u;
     bool alive = true;
 
@@ -240,9 +281,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             if (p < POS) load_dev(d, N, (size_t)gy * nx + ((x0 - 3 + p) % nx + nx) % nx, pre[k]);
         }
     };
-    // features of the prefetched row into input ring row a
+    // features of the prefetched row into input buffer a % 2
     auto store_features = [&](int a) {
-        unsigned char* row = ring_in + (a % 3) * IN_ROW;
+        unsigned char* row = ring_in + (a % 2) * IN_ROW;
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
             const int p = tid + k * TC_THREADS;
@@ -266,64 +307,95 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             *reinterpret_cast<uint4*>(row + PLANE + p * 16) = make_uint4(pack_bf16x2(s_in * v[8], 0.0f), 0u, 0u, 0u);
         }
     };
+    const auto slot = [](int row) { return ((row % 3) + 3) % 3; };
 
-    // Local rows: input a = lattice row ys - 3 + a (0 .. TC_ROWS + 5), layer-1 b (1 .. TC_ROWS + 4)
-    // from input rows b - 1 .. b + 1, layer-2 c (2 .. TC_ROWS + 3), layer-3 e (3 .. TC_ROWS + 2)
-    // = output row ys + e - 3.  Step a computes layer-1 row a - 1, layer-2 row a - 3, layer-3 row
-    // a - 5 in one batch and stores input row a + 1.  Ring row k % 3 of a layer is overwritten by
-    // row k only after the batch that read row k - 3 for the last time has completed.
+    // Local rows: input a = lattice row ys - 3 + a (0 .. TC_ROWS + 5); layer-1 rows 1 .. TC_ROWS + 4,
+    // layer-2 rows 2 .. TC_ROWS + 3 and layer-3 rows 3 .. TC_ROWS + 2 (= output row ys + e - 3) are
+    // the complete ones that the next layer uses; the partial rows at the ends are discarded.
+    // Step a: layer-1 MMAs on input row a, layer-2 MMAs on layer-1 row a - 2, layer-3 MMAs on
+    // layer-2 row a - 4; then layer-1 row a - 1, layer-2 row a - 3 and layer-3 row a - 5 are
+    // complete, read out and their slots zeroed.  A buffer written in step a (layer-1 row a - 1,
+    // layer-2 row a - 3, input row a + 1) was last read by the batch of step a - 1.
     load_row(0);
     store_features(0);
     fence_async_smem();
     __syncthreads();
     constexpr int STEPS = TC_ROWS + 8;
     for (int a = 0; a < STEPS; ++a) {
-        const bool l1 = a >= 2 && a <= TC_ROWS + 5;
-        const bool l2 = a >= 5 && a <= TC_ROWS + 6;
-        const bool l3 = a >= 8;
-        const bool any = l1 || l2 || l3;
-        if (tid == 0 && any) {
+        const bool m1 = a <= TC_ROWS + 5;               // layer-1 MMAs on input row a
+        const bool m2 = a >= 3 && a <= TC_ROWS + 6;     // layer-2 MMAs on layer-1 row a - 2
+        const bool m3 = a >= 6;                         // layer-3 MMAs on layer-2 row a - 4
+        if (tid == 0) {
             fence_after();
-            if (l1) issue_layer<1, 32>(tmem, su32(ring_in), IN_ROW, a - 1, su32(sm + OFF_W1));
-            if (l2) issue_layer<2, 32>(tmem + 32, su32(ring_l1), H_ROW, a - 3, su32(sm + OFF_W2));
-            if (l3) issue_layer<2, 16>(tmem + 64, su32(ring_l2), H_ROW, a - 5, su32(sm + OFF_W3));
+            if (m1) issue_row<1, 32>(tmem + TM_L1, su32(ring_in + (a % 2) * IN_ROW), a, su32(sm + OFF_W1));
+            if (m2) issue_row<2, 32>(tmem + TM_L2, su32(ring_l1 + ((a - 2) % 2) * H_ROW), a - 2, su32(sm + OFF_W2));
+            if (m3) issue_row<2, 16>(tmem + TM_L3, su32(ring_l2 + ((a - 4) % 2) * H_ROW), a - 4, su32(sm + OFF_W3));
             commit(bar);
         }
         const bool next = a + 1 <= TC_ROWS + 5;
         if (next) load_row(a + 1);
-        if (any) {
-            if (tid == 0) s_ok = bar_wait_bounded(bar, parity) ? 1 : 0;
-            __syncthreads();
-            if (!s_ok) {
-                alive = false;
-                break;
-            }
-            bar_try(bar, parity);  // complete: acquire the phase in every thread
-            parity ^= 1u;
-            fence_after();
-            if (l1) {
-                float v[32];
-                tmem_ld32(tmem + lane_off, v);
-                store_hidden(ring_l1 + ((a - 1) % 3) * H_ROW, tid + 1, v, bias);
-            }
-            if (l2) {
-                float v[32];
-                tmem_ld32(tmem + lane_off + 32, v);
-                store_hidden(ring_l2 + ((a - 3) % 3) * H_ROW, tid + 1, v, bias + 32);
-            }
-            if (l3) {
+        if (tid == 0) s_ok = bar_wait_bounded(bar, parity) ? 1 : 0;
+        __syncthreads();
+        if (!s_ok) {
+            alive = false;
+            break;
+        }
+        bar_try(bar, parity);  // complete: acquire the phase in every thread
+        parity ^= 1u;
+        fence_after();
+        if (m1) {  // layer-1 row a - 1 complete (rows 1 .. TC_ROWS + 4 are used)
+            const unsigned t = tmem + lane_off + TM_L1 + 32 * slot(a - 1) + 16 * half;
+            if (a - 1 >= 1) {
                 float v[16];
-                tmem_ld16(tmem + lane_off + 64, v);
-                const int p = tid + 1, oy = ys + a - 8, ox = x0 - 3 + p;
-                if (p >= 3 && p < 3 + OUT_W && ox < nx && oy < ny) {
-                    float4* o = reinterpret_cast<float4*>(y + ((size_t)oy * nx + ox) * 16);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        o[q] = make_float4(v[4 * q] + bias[64 + 4 * q], v[4 * q + 1] + bias[65 + 4 * q],
-                                           v[4 * q + 2] + bias[66 + 4 * q], v[4 * q + 3] + bias[67 + 4 * q]);
+                tmem_ld16(t, v);
+                store_hidden16(ring_l1 + ((a - 1) % 2) * H_ROW, mrow + 1, half, v, bias);
+            }
+            tmem_zero16(t);
+        }
+        if (m2) {  // layer-2 row a - 3 complete (rows 2 .. TC_ROWS + 3 are used)
+            const unsigned t = tmem + lane_off + TM_L2 + 32 * slot(a - 3) + 16 * half;
+            if (a - 3 >= 2) {
+                float v[16];
+                tmem_ld16(t, v);
+                store_hidden16(ring_l2 + ((a - 3) % 2) * H_ROW, mrow + 1, half, v, bias + 32);
+            }
+            tmem_zero16(t);
+        }
+        if (m3) {  // layer-3 row a - 5 complete: output row ys + a - 8 (rows 3 .. TC_ROWS + 2)
+            const int p = mrow + 1, oy = ys + a - 8, ox = x0 - 3 + p;
+            const bool valid = a - 5 >= 3 && p >= 3 && p < 3 + OUT_W && ox < nx && oy < ny;
+            const unsigned t0 = tmem + lane_off + TM_L3 + 16 * slot(a - 5);
+            if (d_next == nullptr) {  // the outputs, split between the warpgroups
+                const unsigned t = t0 + 8 * half;
+                if (a - 5 >= 3) {
+                    float v[8];
+                    tmem_ld8(t, v);
+                    if (valid) {
+                        const float* bb = bias + 64 + 8 * half;
+                        float4* o = reinterpret_cast<float4*>(y + ((size_t)oy * nx + ox) * 16 + 8 * half);
+                        o[0] = make_float4(v[0] + bb[0], v[1] + bb[1], v[2] + bb[2], v[3] + bb[3]);
+                        o[1] = make_float4(v[4] + bb[4], v[5] + bb[5], v[6] + bb[6], v[7] + bb[7]);
+                    }
                 }
+                tmem_zero8(t);
+            } else if (half == 0) {  // the projected correction added to the cell's populations
+                if (a - 5 >= 3) {
+                    float v[16];
+                    tmem_ld16(t0, v);
+                    if (valid) {
+                        float q[9];
+#pragma unroll
+                        for (int i = 0; i < 9; ++i) q[i] = v[i] + bias[64 + i];
+                        project9(q);
+                        const size_t c = (size_t)oy * nx + ox;
+#pragma unroll
+                        for (int i = 0; i < 9; ++i) d_next[c + (size_t)i * N] = d[c + (size_t)i * N] + inv_s_out * q[i];
+                    }
+                }
+                tmem_zero16(t0);
             }
         }
+        tmem_wait_st();
         if (next) store_features(a + 1);
         fence_before();
         fence_async_smem();

@@ -284,3 +284,33 @@ def test_fused_tcgen05_kernel_matches_layer_kernels(gpu, size, form):
     m1 = sim.conservation()
     assert abs(m1[0] - m0[0]) <= 1e-9 * m0[0]
     assert abs(m1[1] - m0[1]) <= 1e-9 * m0[0] and abs(m1[2] - m0[2]) <= 1e-9 * m0[0]
+
+
+@pytest.mark.parametrize("form", FORMS, ids=["-".join(f) for f in FORMS])
+def test_fused_apply_matches_layer_apply(gpu, form):
+    """lbm_closure_apply through the fused kernel -- which adds a per-cell projected correction
+    itself and leaves the corrected state in the lattice's other buffer -- against the layer
+    kernels' apply: the same change of the populations (2e-2 of its largest value), and the
+    lattice steps on from the corrected state."""
+    inputs, target, projection = form
+    nx, ny = 256, 80
+    rng = np.random.default_rng(9)
+    c = Closure(nx, ny, seed=3, s_in=3000.0 if inputs == "neq" else 20.0, s_out=500.0, inputs=inputs, target=target,
+                projection=projection)
+    c.params = _random_params(c, rng)
+    a = _turbulent_sim(nx, ny, 12, steps=10)
+    b = _turbulent_sim(nx, ny, 12, steps=10)
+    f0 = a.read_populations(np.float64)
+    assert np.array_equal(f0, b.read_populations(np.float64))
+    c.set_kernel("layers")
+    c.apply(b)
+    c.set_kernel("fused")
+    c.apply(a)
+    c.status()
+    da, db = a.read_populations(np.float64) - f0, b.read_populations(np.float64) - f0
+    scale = np.max(np.abs(db))
+    assert scale > 0 and np.max(np.abs(da - db)) / scale < 2e-2
+    a.step(5)
+    b.step(5)
+    fa, fb = a.read_populations(np.float64), b.read_populations(np.float64)
+    assert np.max(np.abs(fa - fb)) < 2e-2 * scale + 1e-6
