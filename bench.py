@@ -309,6 +309,54 @@ def run_extras(args, stream, peak):
     res["persistent_over_loop"] = res["persistent"]["glups"] / res["domain_loop"]["glups"]
     b.close()
     out["batch"] = res
+    out["closure"] = closure_speed(stream)
+    return out
+
+
+def closure_speed(stream, nf=4096, factor=4, k_coarse=4):
+    """Speed of the learned-closure form: periodic decaying turbulence, fine lattice nf^2 at tau
+    0.5005 against the coarse lattice (nf / factor)^2 at the acoustically scaled tau with the
+    closure (fused tcgen05 kernel, per-cell projection) applied every k_coarse coarse steps, KBC
+    on both.  Device time per fine step, per coarse step and per closure application (median of
+    repeated intervals); the coarse run covers factor fine steps per coarse step, so its speed-up
+    for the same span is factor * t_fine / (t_coarse + t_closure / k_coarse).  The speed does not
+    depend on the network's weights (seeded initial weights here)."""
+    import numpy as np
+
+    from simuverse_gb300 import FluidSimulator
+    from simuverse_gb300.closure import Closure
+    from simuverse_gb300.turbulence import random_velocity
+
+    nc = nf // factor
+    tau_f = 0.5005
+    tau_c = 0.5 + (tau_f - 0.5) / factor
+    out = {"fine": nf, "coarse": nc, "k_coarse": k_coarse, "collision": "kbc"}
+    sims = {}
+    for name, n, tau in (("fine", nf, tau_f), ("coarse", nc, tau_c)):
+        s = FluidSimulator(n, n, mode="physics", scene="periodic", tau=tau, collision="kbc")
+        ux, uy = random_velocity(n, 9001, 8.0, 0.04)
+        s.init_equilibrium(None, ux.astype(np.float32), uy.astype(np.float32))
+        s.set_stream(stream.cuda_stream)
+        s.step(3)
+        sims[name] = s
+    t_fine = median(timed_intervals(sims["fine"].step, stream, 20, 0.3, min_repeats=3)) / 20
+    t_coarse = median(timed_intervals(sims["coarse"].step, stream, 80, 0.3, min_repeats=3)) / 80
+    c = Closure(nc, nc, seed=1, s_in=20.0, s_out=1e6, inputs="eq", target="populations", projection="cell")
+    c.set_kernel("fused")
+
+    def apply_k(k):
+        for _ in range(k):
+            c.apply(sims["coarse"])
+
+    apply_k(3)
+    t_closure = median(timed_intervals(apply_k, stream, 20, 0.3, min_repeats=3)) / 20
+    c.status()
+    c.close()
+    for s in sims.values():
+        s.close()
+    out.update({"fine_step_ms": t_fine, "coarse_step_ms": t_coarse, "closure_apply_ms": t_closure,
+                "speedup_plain_coarse": factor * t_fine / t_coarse,
+                "speedup_with_closure": factor * t_fine / (t_coarse + t_closure / k_coarse)})
     return out
 
 
@@ -729,7 +777,7 @@ def main():
     ap.add_argument("--rounding", default="nearest", choices=["nearest", "stochastic"],
                     help="rounding of 16-bit population stores")
     ap.add_argument("--workload", default="channel",
-                    choices=["channel", "reference", "precision", "batch", "closure", "view"])
+                    choices=["channel", "reference", "precision", "batch", "closure", "closure_speed", "view"])
     ap.add_argument("--arith", default="fast", choices=["fast", "exact"],
                     help="--workload reference: arithmetic of the reference-rule step")
     ap.add_argument("--train-seeds", type=int, default=8)
@@ -766,6 +814,12 @@ def main():
         run_reference(args)
     elif args.workload == "reference":
         run_reference_rules(args)
+    elif args.workload == "closure_speed":
+        import torch
+
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        print(json.dumps(closure_speed(stream, nf=args.nx)), flush=True)
     elif args.workload == "precision":
         run_precision(args)
     elif args.workload == "batch":
