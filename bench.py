@@ -316,7 +316,7 @@ def run_extras(args, stream, peak):
 def closure_speed(stream, nf=4096, factor=4, k_coarse=4):
     """Speed of the learned-closure form: periodic decaying turbulence, fine lattice nf^2 at tau
     0.5005 against the coarse lattice (nf / factor)^2 at the acoustically scaled tau with the
-    closure (fused tcgen05 kernel, per-cell projection) applied every k_coarse coarse steps, KBC
+    closure (fused tcgen05 kernel, stress form) applied every k_coarse coarse steps, KBC
     on both.  Device time per fine step, per coarse step and per closure application (median of
     repeated intervals); the coarse run covers factor fine steps per coarse step, so its speed-up
     for the same span is factor * t_fine / (t_coarse + t_closure / k_coarse).  The speed does not
@@ -341,7 +341,7 @@ def closure_speed(stream, nf=4096, factor=4, k_coarse=4):
         sims[name] = s
     t_fine = median(timed_intervals(sims["fine"].step, stream, 20, 0.3, min_repeats=3)) / 20
     t_coarse = median(timed_intervals(sims["coarse"].step, stream, 80, 0.3, min_repeats=3)) / 80
-    c = Closure(nc, nc, seed=1, s_in=20.0, s_out=1e6, inputs="eq", target="populations", projection="cell")
+    c = Closure(nc, nc, seed=1, s_in=20.0, s_out=1e6, inputs="eq", target="stress", projection="cell")
     c.set_kernel("fused")
 
     def apply_k(k):
@@ -624,7 +624,10 @@ def run_closure(args):
     out = {"workload": "closure", "fine": args.nx, "coarse": setup.nc, "tau_f": setup.tau_f, "tau_c": setup.tau_c,
            "k_coarse": setup.k_coarse, "collision": args.collision}
     c = Closure(setup.nc, setup.nc, seed=args.seed, inputs=args.inputs, target=args.target, projection=args.projection)
-    out["form"] = {"inputs": args.inputs, "target": args.target, "projection": args.projection}
+    window = args.window or args.k_coarse
+    if args.target == "stress":
+        c.set_stress_factor(window / (2.0 * args.k_coarse))
+    out["form"] = {"inputs": args.inputs, "target": args.target, "projection": args.projection, "window": window}
     out["sources"] = list(args.sources)
     seeds = list(range(1000, 1000 + args.train_seeds))
     npairs = args.train_seeds * args.snapshots * len(args.sources)
@@ -632,11 +635,11 @@ def run_closure(args):
     out["datagen_s"] = 0.0
     out["train_s"] = 0.0
     for rnd in range(1 + args.dagger):
-        c.reserve(npairs + 64, 256, 8)
+        c.reserve(npairs + 64, args.crop, 8)
         t0 = time.perf_counter()
-        generate_pairs(c, setup, seeds, snapshots=args.snapshots, interval=args.interval, crop=256,
+        generate_pairs(c, setup, seeds, snapshots=args.snapshots, interval=args.interval, crop=args.crop,
                        rng_seed=args.seed + rnd, sources=tuple(args.sources), corrected=c if rnd > 0 else None,
-                       calibrate=rnd == 0)
+                       calibrate=rnd == 0, window=window)
         out["datagen_s"] += time.perf_counter() - t0
         hold = max(1, c.npairs // 20)
         if rnd == 0:
@@ -661,7 +664,7 @@ def run_closure(args):
     # seed) by the final velocity error, then used on the evaluation seeds next to strength 1
     best = 1.0
     if len(args.strengths) > 1:
-        rows = evaluate(c, setup, args.val_seed, fine_steps=args.steps, check_every=args.steps,
+        rows = evaluate(c, setup, args.val_seed, fine_steps=args.fine_steps, check_every=args.fine_steps,
                         strengths=tuple(args.strengths))
         last = rows[-1]
         best = min(args.strengths, key=lambda a: last["err_closure" if a == 1.0 else "err_closure@%g" % a])
@@ -669,10 +672,10 @@ def run_closure(args):
     out["strength"] = best
     out["eval"] = {}
     for seed in args.eval_seeds:
-        rows = evaluate(c, setup, seed, fine_steps=args.steps, check_every=args.check_every,
+        rows = evaluate(c, setup, seed, fine_steps=args.fine_steps, check_every=args.check_every,
                         strengths=tuple(sorted({1.0, best})))
         out["eval"][str(seed)] = rows
-    out["timing"] = time_runs(c, setup, args.eval_seeds[0], fine_steps=args.steps, strength=best)
+    out["timing"] = time_runs(c, setup, args.eval_seeds[0], fine_steps=args.fine_steps, strength=best)
     print(json.dumps(out), flush=True)
 
 
@@ -782,10 +785,12 @@ def main():
                     help="--workload reference: arithmetic of the reference-rule step")
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snapshots", type=int, default=125)
-    ap.add_argument("--interval", type=int, default=160)
+    ap.add_argument("--interval", type=int, default=256)
     ap.add_argument("--dagger", type=int, default=0)
     ap.add_argument("--inputs", default="eq", choices=["eq", "neq"])
-    ap.add_argument("--target", default="populations", choices=["momentum", "equilibrium", "populations"])
+    ap.add_argument("--target", default="stress", choices=["momentum", "equilibrium", "populations", "stress"])
+    ap.add_argument("--window", type=int, default=64, help="coarse steps per training pair (0: --k-coarse)")
+    ap.add_argument("--crop", type=int, default=256, help="training crop side (coarse cells)")
     ap.add_argument("--projection", default="cell", choices=["domain", "cell"])
     ap.add_argument("--sources", nargs="+", default=["fresh"], choices=["fresh", "rollout"])
     ap.add_argument("--k-coarse", type=int, default=4)
@@ -797,6 +802,7 @@ def main():
                     help="closure correction strengths tried on the validation seed")
     ap.add_argument("--val-seed", type=int, default=7001)
     ap.add_argument("--check-every", type=int, default=2000)
+    ap.add_argument("--fine-steps", type=int, default=20000, help="--workload closure: fine-equivalent steps evaluated")
     ap.add_argument("--collision", default="kbc", choices=["bgk", "kbc", "mrt", "regularized"])
     ap.add_argument("--taus", type=float, nargs="*", default=[0.51, 0.6, 0.9])
     ap.add_argument("--checkpoints", type=int, nargs="*", default=[1000, 5000])

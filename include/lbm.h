@@ -472,9 +472,20 @@ int lbm_closure_set_scales(lbm_closure* c, float s_in, float s_out);
 #define LBM_CLOSURE_TARGET_POPULATIONS 0
 #define LBM_CLOSURE_TARGET_EQUILIBRIUM 1
 #define LBM_CLOSURE_TARGET_MOMENTUM 2
+/* the stress target (with the per-cell projection only): the correction is a momentum change
+   in flux form, dj(x) = -1/2 sum_i e_i P(y)_i(x - e_i) / s_out, the lattice divergence of the
+   projected outputs, added as 3 w_i e_i . dj -- no cell's density changes and the lattice's
+   total momentum does not either (a divergence sums to zero): a learned sub-grid stress.  The
+   loss compares its effect over the pair's window of n coarse steps with an application every k
+   steps, -factor sum_i e_i P(y)_i(x - e_i) with factor = n / (2 k)
+   (lbm_closure_set_stress_factor), with the momentum difference j(target) - j(pred). */
+#define LBM_CLOSURE_TARGET_STRESS 3
 #define LBM_CLOSURE_PROJECT_CELL 0
 #define LBM_CLOSURE_PROJECT_DOMAIN 1
 int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t projection);
+/* the stress target's factor n / (2 k): window of a pair in coarse steps over twice the
+   interval between applications (default 0.5: one application per step over one step) */
+int lbm_closure_set_stress_factor(lbm_closure* c, float factor);
 /* inference kernel of lbm_closure_apply / lbm_closure_predict: FUSED (default) computes the
    features and the three layers in one kernel on the tcgen05 tensor cores with the activations
    in shared and tensor memory; LAYERS runs the feature kernel and one mma.sync kernel per

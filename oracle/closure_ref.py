@@ -100,6 +100,12 @@ def loss_and_grad(x0, T, params, emulate_bf16=True, project_cell=True):
     count = n * (H - 6) * (W - 6) * 9
     loss = float((e * e).sum() / count)
     gy = (project_t(2.0 * e / count) if project_cell else 2.0 * e / count) * m
+    return loss, backward(x0, x1, x2, gy, params)
+
+
+def backward(x0, x1, x2, gy, params):
+    """Logical gradient vector from the output gradient gy (zero-padded convolutions)."""
+    W1, b1, W2, b2, W3, b3 = unpack(params)
 
     def dweights(x, g):
         dW = np.stack([shift(x, t // 3 - 1, t % 3 - 1, False).reshape(-1, x.shape[-1]).T @ g.reshape(-1, g.shape[-1])
@@ -117,4 +123,32 @@ def loss_and_grad(x0, T, params, emulate_bf16=True, project_cell=True):
     dW2, db2 = dweights(x1, g2)
     g1 = dinput(g2, W2) * (x1 > 0)
     dW1, db1 = dweights(x0, g1)
-    return loss, pack(dW1, db1, dW2, db2, dW3, db3)
+    return pack(dW1, db1, dW2, db2, dW3, db3)
+
+
+def stress_loss_and_grad(x0, T, params, factor, emulate_bf16=True):
+    """The stress target's loss (lbm_closure.cu k_stress_residual / k_stress_grad): over the
+    interior [4, S-4)^2, r = -factor sum_i e_i P(y)_i(x - e_i) - sum_i e_i T_i(x); mean of
+    |r|^2 over the interior's cells and both components, and the logical gradient vector."""
+    x0, x1, x2, y = forward(x0, params, False, emulate_bf16)
+    n, H, W, _ = y.shape
+    T = bf16(T) if emulate_bf16 else T
+    Py = project(y)
+    mx = np.zeros((n, H, W))
+    my = np.zeros((n, H, W))
+    for i in range(1, 9):  # P(y)_i of the cell x - e_i: shift by -e_i
+        s = shift(Py[..., i:i + 1], -int(EY[i]), -int(EX[i]), False)[..., 0]
+        mx += EX[i] * s
+        my += EY[i] * s
+    mask = np.zeros((n, H, W))
+    mask[:, 4:H - 4, 4:W - 4] = 1.0
+    rx = (-factor * mx - (T * EX).sum(-1)) * mask
+    ry = (-factor * my - (T * EY).sum(-1)) * mask
+    count = n * (H - 8) * (W - 8) * 2
+    loss = float(((rx * rx) + (ry * ry)).sum() / count)
+    g = np.zeros_like(y)
+    for i in range(1, 9):  # r at x + e_i: shift by +e_i
+        sx = shift(rx[..., None], int(EY[i]), int(EX[i]), False)[..., 0]
+        sy = shift(ry[..., None], int(EY[i]), int(EX[i]), False)[..., 0]
+        g[..., i] = -factor * 2.0 / count * (EX[i] * sx + EY[i] * sy)
+    return loss, backward(x0, x1, x2, project_t(g), params)

@@ -148,6 +148,7 @@ _SIGNATURES = {
     "lbm_closure_set_scales": [_P, _F, _F],
     "lbm_closure_set_form": [_P, _I, _I, _I],
     "lbm_closure_set_kernel": [_P, _I],
+    "lbm_closure_set_stress_factor": [_P, _F],
     "lbm_closure_status": [_P],
     "lbm_closure_get_params": [_P, _P],
     "lbm_closure_set_params": [_P, _P],

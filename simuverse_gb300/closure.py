@@ -21,7 +21,7 @@ def coarsen(fine, coarse, factor: int, neq_scale: float):
 
 class Closure:
     INPUTS = {"neq": 0, "eq": 1}
-    TARGETS = {"populations": 0, "equilibrium": 1, "momentum": 2}
+    TARGETS = {"populations": 0, "equilibrium": 1, "momentum": 2, "stress": 3}
     PROJECTIONS = {"cell": 0, "domain": 1}
 
     def __init__(self, nx: int, ny: int, seed: int = 0, s_in: float = 1000.0, s_out: float = 1000.0,
@@ -58,6 +58,11 @@ class Closure:
         nat.check(self._lib.lbm_closure_set_form(self._h, self.INPUTS[inputs], self.TARGETS[target],
                                                  self.PROJECTIONS[projection]))
         self.inputs, self.target, self.projection = inputs, target, projection
+
+    def set_stress_factor(self, factor: float):
+        """Stress target: window of a pair in coarse steps / (2 x steps between applications)."""
+        nat.check(self._lib.lbm_closure_set_stress_factor(self._h, float(factor)))
+        self.stress_factor = float(factor)
 
     KERNELS = {"fused": 0, "layers": 1}
 
@@ -194,7 +199,7 @@ def _project(v):
 
 
 def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256, rng_seed=0, log=None,
-                   sources=("fresh", "rollout"), corrected=None, calibrate=True):
+                   sources=("fresh", "rollout"), corrected=None, calibrate=True, window=None):
     """Training pairs from `snapshots` snapshots of every seed, taken every `interval` fine
     steps over one fine run.  Each snapshot adds one pair per source:
 
@@ -203,12 +208,21 @@ def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256,
       initial state -- with the closure `corrected` applied every k_coarse coarse steps when
       given, as in evaluation -- so the pairs cover the states a long coarse run reaches.
 
-    The target is the coarse-grained fine state at the same time.  With `calibrate`, the
+    The target is the coarse-grained fine state at the same time.  A pair spans `window`
+    coarse steps (default: the closure's interval k_coarse; the stress target learns from
+    longer windows, over which its momentum effect accumulates).  With `calibrate`, the
     feature and output scales are set from the first fresh pair (unit RMS)."""
     rng = np.random.default_rng(rng_seed)
     pred, target = setup.coarse(), setup.coarse()
-    kf = setup.k_coarse * setup.factor
+    w = setup.k_coarse if window is None else int(window)
+    kf = w * setup.factor
     assert interval % kf == 0 and interval >= kf
+
+    def roll_steps(roll, n):  # n coarse steps, the closure `corrected` every k_coarse of them
+        for _ in range(n // setup.k_coarse):
+            roll.step(setup.k_coarse)
+            if corrected is not None:
+                corrected.apply(roll)
     calibrated = not calibrate
     for seed in seeds:
         fine = setup.fine(seed)
@@ -219,9 +233,9 @@ def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256,
         for s in range(snapshots):
             if "fresh" in sources:
                 coarsen(fine, pred, setup.factor, setup.neq_scale)
-                pred.step(setup.k_coarse)
+                pred.step(w)
             if roll is not None:
-                roll.step(setup.k_coarse)
+                roll_steps(roll, w)
             fine.step(kf)
             coarsen(fine, target, setup.factor, setup.neq_scale)
             if not calibrated:
@@ -231,12 +245,12 @@ def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256,
                 feat = neq if closure.inputs == "neq" else (fp - _W9[:, None, None]) - neq
                 if closure.target == "equilibrium":
                     tgt = (ft - _neq_and_momentum(ft)[0]) - (fp - neq)
-                elif closure.target == "momentum":
+                elif closure.target in ("momentum", "stress"):
                     dj = ((ft - fp) * _EX[:, None, None]).sum(0), ((ft - fp) * _EY[:, None, None]).sum(0)
                     tgt = 3.0 * _W9[:, None, None] * (_EX[:, None, None] * dj[0] + _EY[:, None, None] * dj[1])
                 else:
                     tgt = ft - fp
-                if closure.projection == "cell":
+                if closure.projection == "cell" and closure.target != "stress":
                     tgt = _project(tgt)
                 closure.set_scales(1.0 / max(float(feat.std()), 1e-12), 1.0 / max(float(tgt.std()), 1e-12))
                 calibrated = True
@@ -245,12 +259,7 @@ def generate_pairs(closure, setup, seeds, snapshots=125, interval=160, crop=256,
                 closure.add_pair(pred, target, ox, oy)
             if roll is not None:
                 closure.add_pair(roll, target, ox, oy)
-                if corrected is not None:
-                    corrected.apply(roll)
-                for _ in range((interval - kf) // kf):
-                    roll.step(setup.k_coarse)
-                    if corrected is not None:
-                        corrected.apply(roll)
+                roll_steps(roll, (interval - kf) // setup.factor)
             fine.step(interval - kf)
         if log:
             log("seed %d: %d pairs" % (seed, closure.npairs))

@@ -238,6 +238,49 @@ __global__ void k_apply(const float* __restrict__ y, float* __restrict__ d, int 
     }
 }
 
+// The stress target's correction, a momentum change in flux form: dj(x) = -1/2 sum_i e_i
+// z_i(x - e_i) / s_out over the periodic field, z = P(y) as 9 planes of nx * ny floats, added
+// to the cell's populations as 3 w_i e_i . dj.  No cell's density changes; the lattice's total
+// momentum does not either (a lattice divergence sums to zero).  accumulate: d += delta, else
+// d = delta (9 planes)
+__global__ void k_apply_stress(const float* __restrict__ z, float* __restrict__ d, int nx, int ny, float inv_s_out,
+                               int accumulate) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (x >= nx) return;
+    const size_t N = (size_t)nx * ny, c = (size_t)r * nx + x;
+    float jx = 0.0f, jy = 0.0f;
+#pragma unroll
+    for (int i = 1; i < 9; ++i) {  // population i of the source cell x - e_i
+        const int sx = x - EX(i) < 0 ? nx - 1 : (x - EX(i) >= nx ? 0 : x - EX(i));
+        const int sy = r - EY(i) < 0 ? ny - 1 : (r - EY(i) >= ny ? 0 : r - EY(i));
+        const float v = z[(size_t)i * N + (size_t)sy * nx + sx];
+        jx += (float)EX(i) * v;
+        jy += (float)EY(i) * v;
+    }
+    jx *= -0.5f * inv_s_out;
+    jy *= -0.5f * inv_s_out;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const float delta = 3.0f * PW<float>(i) * ((float)EX(i) * jx + (float)EY(i) * jy);
+        if (accumulate)
+            d[c + i * N] += delta;
+        else
+            d[c + i * N] = delta;
+    }
+}
+
+// P(y) of every cell of a field (y: [N][16] f32) into 9 planes of N floats
+__global__ void k_project_planes(const float* __restrict__ y, size_t N, float* __restrict__ z) {
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = y[c * 16 + k];
+    project9(v);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) z[(size_t)k * N + c] = v[k];
+}
+
 // loss over the interior [3, H-3) x [3, W-3) of every image and the output gradient
 // g = P^T(2 (P(y) - T) / count) (zero outside the interior), or without P when project_cell
 // is 0; per-block FP64 loss partials
@@ -277,6 +320,80 @@ __global__ void k_loss(const float* __restrict__ y, const __nv_bfloat16* __restr
         double s = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
         part[blockIdx.x] = s;
+    }
+}
+
+// Stress target (LBM_CLOSURE_TARGET_STRESS).  Each application changes a cell's momentum by the
+// lattice divergence of the projected outputs, -1/2 sum_i e_i P(y)_i(x - e_i) / s_out
+// (k_apply_stress); over a pair's window of n coarse steps with an application every k steps the
+// model is m(x) = -factor sum_i e_i P(y)_i(x - e_i) in output units, factor = n / (2 k).
+// Pass 1: over the cells [4, H-4) x [4, W-4) of every image the residual r = m - T_j, T_j =
+// sum_i e_i T_i the stored momentum target, into res (zero elsewhere), FP64 loss partials.
+__global__ void k_stress_residual(const float* __restrict__ y, const __nv_bfloat16* __restrict__ T, int nimg, int H,
+                                  int W, float factor, float2* __restrict__ res, double* __restrict__ part) {
+    __shared__ double red[32];
+    const size_t total = (size_t)nimg * H * W;
+    double acc = 0.0;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % W), r = (int)((c / W) % H);
+        if (x < 4 || x >= W - 4 || r < 4 || r >= H - 4) {
+            res[c] = make_float2(0.0f, 0.0f);
+            continue;
+        }
+        float mx = 0.0f, my = 0.0f;
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {  // P(y) of the source cell x - e_i, its population i
+            const long src = (long)c - (long)EY(i) * W - EX(i);
+            float v[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) v[k] = y[(size_t)src * 16 + k];
+            project9(v);
+            mx += (float)EX(i) * v[i];
+            my += (float)EY(i) * v[i];
+        }
+        float tx = 0.0f, ty = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const float t = __bfloat162float(T[c * 16 + i]);
+            tx += (float)EX(i) * t;
+            ty += (float)EY(i) * t;
+        }
+        const float rx = -factor * mx - tx, ry = -factor * my - ty;
+        res[c] = make_float2(rx, ry);
+        acc += (double)rx * rx + (double)ry * ry;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// pass 2: the output gradient g(x) = P^T(h), h_i = -factor * 2 inv_count * e_i . r(x + e_i)
+// (r zero outside its cells and outside the image), BF16 into g (16 channels)
+__global__ void k_stress_grad(const float2* __restrict__ res, int nimg, int H, int W, float factor, float inv_count,
+                              __nv_bfloat16* __restrict__ g) {
+    const size_t total = (size_t)nimg * H * W;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % W), r = (int)((c / W) % H);
+        float h[9];
+        h[0] = 0.0f;
+#pragma unroll
+        for (int i = 1; i < 9; ++i) {
+            const int xx = x + EX(i), rr = r + EY(i);
+            float2 q = make_float2(0.0f, 0.0f);
+            if (xx >= 0 && xx < W && rr >= 0 && rr < H) q = res[(long)c + (long)EY(i) * W + EX(i)];
+            h[i] = -factor * 2.0f * inv_count * ((float)EX(i) * q.x + (float)EY(i) * q.y);
+        }
+        project9_t(h);
+        unsigned* go = reinterpret_cast<unsigned*>(g + c * 16);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) go[k] = pack_bf16x2(h[2 * k], h[2 * k + 1]);
+        go[4] = pack_bf16x2(h[8], 0.0f);
+        go[5] = go[6] = go[7] = 0u;
     }
 }
 
@@ -384,6 +501,9 @@ struct lbm_closure {
     int target = LBM_CLOSURE_TARGET_POPULATIONS;
     int projection = LBM_CLOSURE_PROJECT_CELL;
     int kernel = LBM_CLOSURE_KERNEL_FUSED;  // inference: one tcgen05 kernel, or the three layer kernels
+    float stress_factor = 0.5f;             // stress target: window / (2 x application interval)
+    float* bres = nullptr;                  // stress target: residuals of a batch (2 floats per cell)
+    float* zp = nullptr;                    // stress target: P(y) of the field, 9 planes
     int* d_status = nullptr;                // LBM_ERR_TIMEOUT from a bounded wait of the fused kernel
     double* dmeans = nullptr;  // reduction partials (RED_BLOCKS x 3) and the 3 field means
     int device = 0;
@@ -503,11 +623,23 @@ int dweight(lbm_closure* c, const __nv_bfloat16* x, const GT* gr, int nimg, int 
     return LBM_OK;
 }
 
-// gradient of the mean loss of the batch in c->bx0 / c->bt (nimg crops) into c->g;
-// loss into c->dloss (device)
-int loss_and_grad(lbm_closure* c, int nimg) {
+// the mean loss of the network outputs c->by against the targets c->bt (nimg crops) into
+// c->dloss (device) and the output gradient into c->bg3
+int batch_loss(lbm_closure* c, int nimg) {
     const int S = c->crop;
-    C_TRY(forward<false>(c, c->bx0, c->bx1, c->bx2, c->by, nimg, S, S));
+    if (c->target == LBM_CLOSURE_TARGET_STRESS) {
+        const double count = (double)nimg * (S - 8) * (S - 8) * 2.0;
+        cl::k_stress_residual<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, nimg, S, S, c->stress_factor,
+                                                                        reinterpret_cast<float2*>(c->bres), c->lpart);
+        C_CK(cudaGetLastError());
+        cl::k_stress_grad<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(reinterpret_cast<const float2*>(c->bres), nimg, S, S,
+                                                                    c->stress_factor, (float)(1.0 / count), c->bg3);
+        C_CK(cudaGetLastError());
+        cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
+        C_CK(cudaGetLastError());
+        c->launches += 3;
+        return LBM_OK;
+    }
     const double count = (double)nimg * (S - 6) * (S - 6) * 9.0;
     cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, nimg, S, S, (float)(1.0 / count),
                                                          c->projection == LBM_CLOSURE_PROJECT_CELL, c->bg3, c->lpart);
@@ -515,6 +647,15 @@ int loss_and_grad(lbm_closure* c, int nimg) {
     cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
     C_CK(cudaGetLastError());
     c->launches += 2;
+    return LBM_OK;
+}
+
+// gradient of the mean loss of the batch in c->bx0 / c->bt (nimg crops) into c->g;
+// loss into c->dloss (device)
+int loss_and_grad(lbm_closure* c, int nimg) {
+    const int S = c->crop;
+    C_TRY(forward<false>(c, c->bx0, c->bx1, c->bx2, c->by, nimg, S, S));
+    C_TRY(batch_loss(c, nimg));
     // layer 3: dW3, db3 from x2 and g3; g2 = conv_bwd3(g3) masked by x2 > 0; and so on down
     C_TRY((dweight<32, 16, __nv_bfloat16>(c, c->bx2, c->bg3, nimg, S, S, c->g + cl::OW3)));
     C_TRY((conv<16, 32, cl::EPI_MASK, false>(c, c->bg3, c->bg2, c->wb3, nullptr, c->bx2, nimg, S, S)));
@@ -577,6 +718,7 @@ int lbm_closure_create(int32_t nx, int32_t ny, uint64_t seed, lbm_closure** out)
     if (e == cudaSuccess) e = dalloc(&c->dloss, 8);
     if (e == cudaSuccess) e = dalloc(&c->dwpart, (size_t)cl::DW_BLOCKS * (9 * 32 * 32 + 32));
     if (e == cudaSuccess) e = dalloc(&c->d_status, 1);
+    if (e == cudaSuccess) e = dalloc(&c->zp, N * 9);
     if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
         lbm_closure_destroy(c);
@@ -618,7 +760,7 @@ int lbm_closure_destroy(lbm_closure* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->p,  c->g,  c->m,   c->v,   c->mask, c->wf1, c->wf2, c->wf3, c->wb3, c->wb2, c->x0,
                     c->x1, c->x2, c->y,   c->dsx, c->dst,  c->bx0, c->bt,  c->bx1, c->bx2, c->bg3, c->bg2,
-                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans, c->d_status};
+                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans, c->d_status, c->bres, c->zp};
     for (void* b : bufs) cudaFree(b);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -638,8 +780,10 @@ int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t
     if (inputs != LBM_CLOSURE_INPUT_NEQ && inputs != LBM_CLOSURE_INPUT_EQ)
         return cfail(LBM_ERR_ARG, "unknown closure input mode %d", inputs);
     if (target != LBM_CLOSURE_TARGET_POPULATIONS && target != LBM_CLOSURE_TARGET_EQUILIBRIUM &&
-        target != LBM_CLOSURE_TARGET_MOMENTUM)
+        target != LBM_CLOSURE_TARGET_MOMENTUM && target != LBM_CLOSURE_TARGET_STRESS)
         return cfail(LBM_ERR_ARG, "unknown closure target %d", target);
+    if (target == LBM_CLOSURE_TARGET_STRESS && projection != LBM_CLOSURE_PROJECT_CELL)
+        return cfail(LBM_ERR_ARG, "the stress target acts through the per-cell projection");
     if (projection != LBM_CLOSURE_PROJECT_CELL && projection != LBM_CLOSURE_PROJECT_DOMAIN)
         return cfail(LBM_ERR_ARG, "unknown closure projection %d", projection);
     if (target == LBM_CLOSURE_TARGET_MOMENTUM && projection == LBM_CLOSURE_PROJECT_CELL)
@@ -647,6 +791,13 @@ int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t
     c->inputs = inputs;
     c->target = target;
     c->projection = projection;
+    return LBM_OK;
+}
+
+int lbm_closure_set_stress_factor(lbm_closure* c, float factor) {
+    C_TRY(check_closure(c));
+    if (!(factor > 0.0f) || !std::isfinite(factor)) return cfail(LBM_ERR_ARG, "the stress factor must be positive");
+    c->stress_factor = factor;
     return LBM_OK;
 }
 
@@ -723,14 +874,15 @@ int correction(lbm_closure* c, lbm_handle* h, float* out, int accumulate) {
             &done);
         // applying a per-cell projected correction needs no field reduction: the kernel adds it
         // itself and writes the corrected state into the lattice's other buffer
-        const bool in_kernel = accumulate && out == (float*)h->buf[h->cur] && c->projection == LBM_CLOSURE_PROJECT_CELL;
+        const bool in_kernel = accumulate && out == (float*)h->buf[h->cur] &&
+                               c->projection == LBM_CLOSURE_PROJECT_CELL && c->target != LBM_CLOSURE_TARGET_STRESS;
         if (e == cudaSuccess) {
             const dim3 grid((unsigned)((c->nx + cl::tc::OUT_W - 1) / cl::tc::OUT_W),
                             (unsigned)((c->ny + cl::tc::TC_ROWS - 1) / cl::tc::TC_ROWS));
             cl::tc::k_closure_fused<<<grid, cl::tc::TC_THREADS, cl::tc::SMEM_BYTES, s>>>(
                 (const float*)h->buf[h->cur], c->nx, c->ny, c->s_in, c->inputs, c->wf1, c->wf2, c->wf3, c->p + cl::OB1,
                 c->p + cl::OB2, c->p + cl::OB3, c->y, in_kernel ? (float*)h->buf[h->cur ^ 1] : nullptr,
-                1.0f / c->s_out, c->d_status);
+                1.0f / c->s_out, c->target == LBM_CLOSURE_TARGET_STRESS ? c->zp : nullptr, c->d_status);
             e = cudaGetLastError();
             ++c->launches;
         }
@@ -758,7 +910,16 @@ int correction(lbm_closure* c, lbm_handle* h, float* out, int accumulate) {
         e = cudaGetLastError();
         if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "field means: %s", cudaGetErrorString(e));
     }
-    if (r == LBM_OK) {
+    if (r == LBM_OK && c->target == LBM_CLOSURE_TARGET_STRESS) {
+        if (c->kernel != LBM_CLOSURE_KERNEL_FUSED) {  // the fused kernel writes the planes itself
+            const size_t N = (size_t)c->nx * c->ny;
+            cl::k_project_planes<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(c->y, N, c->zp);
+            ++c->launches;
+        }
+        cl::k_apply_stress<<<g1, 128, 0, s>>>(c->zp, out, c->nx, c->ny, 1.0f / c->s_out, accumulate);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "apply: %s", cudaGetErrorString(e));
+    } else if (r == LBM_OK) {
         cl::k_apply<<<g1, 128, 0, s>>>(c->y, out, c->nx, c->ny, 1.0f / c->s_out, means, accumulate);
         e = cudaGetLastError();
         if (e != cudaSuccess) r = cfail(LBM_ERR_CUDA, "apply: %s", cudaGetErrorString(e));
@@ -779,9 +940,9 @@ int lbm_closure_apply(lbm_closure* c, lbm_handle* h) {
     C_CK(cudaSetDevice(c->device));
     const int r = correction(c, h, (float*)h->buf[h->cur], 1);
     if (c->kernel == LBM_CLOSURE_KERNEL_FUSED)  // one kernel, plus the field means and the apply pass
-        h->launches += c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 4 : 1;
+        h->launches += c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 4 : (c->target == LBM_CLOSURE_TARGET_STRESS ? 2 : 1);
     else
-        h->launches += 4 + (c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 3 : 1);
+        h->launches += 4 + (c->projection == LBM_CLOSURE_PROJECT_DOMAIN ? 3 : (c->target == LBM_CLOSURE_TARGET_STRESS ? 2 : 1));
     return r;
 }
 
@@ -816,6 +977,8 @@ int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t
     }
     cudaFree(c->by);
     c->by = nullptr;
+    cudaFree(c->bres);
+    c->bres = nullptr;
     const size_t cs = (size_t)crop * crop;
     C_CK(dalloc(&c->dsx, (size_t)max_pairs * cs * 16));
     C_CK(dalloc(&c->dst, (size_t)max_pairs * cs * 16));
@@ -827,6 +990,7 @@ int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t
     C_CK(dalloc(&c->bg2, (size_t)batch * cs * 32));
     C_CK(dalloc(&c->bg1, (size_t)batch * cs * 32));
     C_CK(dalloc(&c->by, (size_t)batch * cs * 16));
+    C_CK(dalloc(&c->bres, (size_t)batch * cs * 2));
     c->cap = max_pairs;
     c->crop = crop;
     c->batch = batch;
@@ -852,8 +1016,12 @@ int lbm_closure_add_pair(lbm_closure* c, lbm_handle* pred, lbm_handle* target, i
     cl::k_features<<<g, 128, 0, c->stream>>>((const float*)pred->buf[pred->cur], pred->nx, pred->ny, x, y, S, S,
                                              c->s_in, c->inputs, c->dsx + off);
     cl::k_target<<<g, 128, 0, c->stream>>>((const float*)target->buf[target->cur], (const float*)pred->buf[pred->cur],
-                                           pred->nx, pred->ny, x, y, S, S, c->s_out, c->target,
-                                           c->projection == LBM_CLOSURE_PROJECT_CELL, c->dst + off);
+                                           pred->nx, pred->ny, x, y, S, S, c->s_out,
+                                           c->target == LBM_CLOSURE_TARGET_STRESS ? LBM_CLOSURE_TARGET_MOMENTUM
+                                                                                  : c->target,
+                                           c->projection == LBM_CLOSURE_PROJECT_CELL &&
+                                               c->target != LBM_CLOSURE_TARGET_STRESS,
+                                           c->dst + off);
     C_CK(cudaGetLastError());
     c->launches += 2;
     ++c->npairs;
@@ -914,12 +1082,7 @@ int lbm_closure_eval(lbm_closure* c, int32_t begin, int32_t end, double* loss_ou
         C_CK(cudaMemcpyAsync(c->bx0, c->dsx + k0 * img, B * img * 2, cudaMemcpyDeviceToDevice, c->stream));
         C_CK(cudaMemcpyAsync(c->bt, c->dst + k0 * img, B * img * 2, cudaMemcpyDeviceToDevice, c->stream));
         C_TRY(forward<false>(c, c->bx0, c->bx1, c->bx2, c->by, B, S, S));
-        const double count = (double)B * (S - 6) * (S - 6) * 9.0;
-        cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, B, S, S, (float)(1.0 / count),
-                                                             c->projection == LBM_CLOSURE_PROJECT_CELL, c->bg3,
-                                                             c->lpart);
-        cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
-        C_CK(cudaGetLastError());
+        C_TRY(batch_loss(c, B));
         double l = 0.0;
         C_CK(cudaMemcpyAsync(&l, c->dloss, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         C_CK(cudaStreamSynchronize(c->stream));

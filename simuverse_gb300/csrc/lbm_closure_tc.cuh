@@ -197,14 +197,15 @@ __device__ __forceinline__ void issue_row(unsigned dtmem, unsigned in_row, int r
 // cin); b1 [32], b2 [32], b3 [16] FP32.  With d_next == nullptr the outputs go to y ([nx * ny][16]
 // FP32, 9 used); otherwise the correction is applied here: d_next = d + inv_s_out * P(y) cell by
 // cell (P removes a cell's density and momentum), d_next being a buffer other than d (the CTAs
-// read each other's halo rows of d).
+// read each other's halo rows of d).  With zp != nullptr (and d_next == nullptr) the outputs go
+// projected, P(y), to 9 planes of nx * ny floats instead of y.
 // Grid (ceil(nx / OUT_W), ceil(ny / TC_ROWS)), TC_THREADS threads, SMEM_BYTES dynamic shared memory.
 __global__ void __launch_bounds__(TC_THREADS, 2)
     k_closure_fused(const float* __restrict__ d, int nx, int ny, float s_in, int inputs,
                     const __nv_bfloat16* __restrict__ w1, const __nv_bfloat16* __restrict__ w2,
                     const __nv_bfloat16* __restrict__ w3, const float* __restrict__ b1, const float* __restrict__ b2,
                     const float* __restrict__ b3, float* __restrict__ y, float* __restrict__ d_next, float inv_s_out,
-                    int* __restrict__ status) {
+                    float* __restrict__ zp, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             const int p = mrow + 1, oy = ys + a - 8, ox = x0 - 3 + p;
             const bool valid = a - 5 >= 3 && p >= 3 && p < 3 + OUT_W && ox < nx && oy < ny;
             const unsigned t0 = tmem + lane_off + TM_L3 + 16 * slot(a - 5);
-            if (d_next == nullptr) {  // the outputs, split between the warpgroups
+            if (d_next == nullptr && zp == nullptr) {  // the outputs, split between the warpgroups
                 const unsigned t = t0 + 8 * half;
                 if (a - 5 >= 3) {
                     float v[8];
@@ -378,7 +379,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
                     }
                 }
                 tmem_zero8(t);
-            } else if (half == 0) {  // the projected correction added to the cell's populations
+            } else if (half == 0) {  // the projected outputs: added to the populations, or as planes
                 if (a - 5 >= 3) {
                     float v[16];
                     tmem_ld16(t0, v);
@@ -388,8 +389,14 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
                         for (int i = 0; i < 9; ++i) q[i] = v[i] + bias[64 + i];
                         project9(q);
                         const size_t c = (size_t)oy * nx + ox;
+                        if (d_next != nullptr) {
 #pragma unroll
-                        for (int i = 0; i < 9; ++i) d_next[c + (size_t)i * N] = d[c + (size_t)i * N] + inv_s_out * q[i];
+                            for (int i = 0; i < 9; ++i)
+                                d_next[c + (size_t)i * N] = d[c + (size_t)i * N] + inv_s_out * q[i];
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 9; ++i) zp[c + (size_t)i * N] = q[i];
+                        }
                     }
                 }
                 tmem_zero16(t0);

@@ -204,27 +204,34 @@ def test_training_reduces_the_loss(gpu):
     assert l1 < 0.8 * l0, (l0, l1)
 
 
-def test_closure_gain_over_plain_coarse_run_is_measured(gpu):
+def test_closure_gains_over_plain_coarse_run(gpu):
     """What the trained network gains over the coarse run without it, on a small decaying-
-    turbulence case (fine 512^2, coarse 128^2): the closure-corrected run stays finite and within
-    a factor of the uncorrected run's error, and both errors are reported."""
+    turbulence case (fine 512^2, coarse 128^2, tau 0.5005, KBC on both, unseen seed 9001): the
+    stress form -- a flux-form momentum correction every 4 coarse steps, trained on the
+    momentum difference over 32-coarse-step windows -- lowers the coarse run's relative L2
+    velocity error against the coarse-grained fine run after 2048 fine steps by more than 15 %
+    (measured 9.1 % against 12.9 %)."""
     from simuverse_gb300.closure import TurbulenceSetup, evaluate, generate_pairs
 
     setup = TurbulenceSetup(nf=512, factor=4, tau_f=0.5005, k_coarse=4, collision="kbc")
-    c = Closure(setup.nc, setup.nc, seed=0, inputs="eq", target="populations", projection="cell")
+    c = Closure(setup.nc, setup.nc, seed=0, inputs="eq", target="stress", projection="cell")
+    c.set_stress_factor(32 / (2.0 * setup.k_coarse))
     c.reserve(8 * 20 + 8, 64, 8)
-    generate_pairs(c, setup, list(range(1000, 1008)), snapshots=20, interval=160, crop=64, rng_seed=0,
-                   sources=("fresh",))
+    generate_pairs(c, setup, list(range(1000, 1008)), snapshots=20, interval=256, crop=64, rng_seed=0,
+                   sources=("fresh",), window=32)
     assert c.npairs == 160
-    l0 = c.eval(c.npairs - 8, c.npairs)
-    c.train(400, lr=1e-3, seed=1)
-    assert c.eval(c.npairs - 8, c.npairs) < l0
+    hold = 8
+    l0 = c.eval(c.npairs - hold, c.npairs)
+    for b in range(10):
+        c.train(200, lr=1e-3 if b < 8 else 2.5e-4, seed=b)
+    l1 = c.eval(c.npairs - hold, c.npairs)
+    assert l1 < 0.8 * l0, (l0, l1)
     rows = evaluate(c, setup, 9001, fine_steps=2048, check_every=1024)
     last = rows[-1]
     print("closure %.4f vs plain %.4f relative L2 velocity error after %d fine steps"
           % (last["err_closure"], last["err_plain"], last["fine_step"]))
-    assert np.isfinite(last["err_closure"]) and last["fine_nonfinite"] == 0
-    assert last["err_closure"] < 1.5 * last["err_plain"] + 1e-3
+    assert last["fine_nonfinite"] == 0 and np.isfinite(last["err_closure"])
+    assert last["err_closure"] < 0.85 * last["err_plain"], (last["err_closure"], last["err_plain"])
     c.close()
 
 
@@ -314,3 +321,59 @@ def test_fused_apply_matches_layer_apply(gpu, form):
     b.step(5)
     fa, fb = a.read_populations(np.float64), b.read_populations(np.float64)
     assert np.max(np.abs(fa - fb)) < 2e-2 * scale + 1e-6
+
+
+def test_stress_target_gradients_match_fp64_restatement(gpu):
+    """The stress target's loss and parameter gradient (k_stress_residual, k_stress_grad and the
+    network backward) against the FP64 restatement with BF16 emulation."""
+    rng = np.random.default_rng(4)
+    c = Closure(64, 64, seed=2, inputs="eq", target="stress", projection="cell")
+    c.set_stress_factor(4.0)
+    c.params = _random_params(c, rng)
+    c.reserve(4, 32, 2)
+    feats = rng.standard_normal((2, 32, 32, 9))
+    targets = 0.3 * rng.standard_normal((2, 32, 32, 9))
+    loss, g = c.loss_grad(feats, targets)
+    loss_ref, g_ref = ref.stress_loss_and_grad(feats, targets, c.params, 4.0, emulate_bf16=True)
+    assert abs(loss - loss_ref) / loss_ref < 1e-2, (loss, loss_ref)
+    # the last layer's bias adds the same vector to every cell, whose projection has no lattice
+    # divergence: the loss does not depend on it, and both gradients are rounding noise
+    b3_gpu, b3_ref = g[-9:].astype(np.float64), g_ref[-9:]
+    scale = np.linalg.norm(g_ref[-(9 + 9 * 32 * 9):-9])
+    assert np.linalg.norm(b3_gpu) < 1e-3 * scale and np.linalg.norm(b3_ref) < 1e-6 * scale
+    off = 0
+    for n in (9 * 9 * 32, 32, 9 * 32 * 32, 32, 9 * 32 * 9):
+        a, b = g[off:off + n].astype(np.float64), g_ref[off:off + n]
+        off += n
+        rel = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
+        assert rel < 5e-2 and cos > 0.998, (n, rel, cos)
+
+
+def test_stress_form_rejects_field_projection(gpu):
+    with pytest.raises(Exception):
+        Closure(64, 64, seed=2, inputs="eq", target="stress", projection="domain")
+
+
+def test_stress_correction_is_a_momentum_flux(gpu):
+    """The stress form's correction changes no cell's density, conserves the lattice's total
+    momentum, and changes a cell's momentum by -1/2 sum_i e_i P(y)_i(x - e_i) / s_out (checked
+    against the predicted correction of the layer kernels and a numpy divergence of the
+    fused kernel's outputs)."""
+    nx, ny = 128, 64
+    rng = np.random.default_rng(21)
+    c = Closure(nx, ny, seed=4, s_in=20.0, s_out=300.0, inputs="eq", target="stress", projection="cell")
+    c.params = _random_params(c, rng)
+    sim = _turbulent_sim(nx, ny, 13, steps=10)
+    delta = c.predict(sim).astype(np.float64)
+    assert np.max(np.abs(delta.sum(0))) < 1e-9 + 1e-6 * np.max(np.abs(delta))
+    djx = (delta * ref.EX[:, None, None]).sum(0)
+    assert abs(djx.sum()) < 1e-4 * np.abs(djx).sum()
+    c.set_kernel("layers")
+    d2 = c.predict(sim).astype(np.float64)
+    assert np.max(np.abs(delta - d2)) < 2e-2 * np.max(np.abs(d2))
+    m0 = sim.conservation()
+    c.apply(sim)
+    m1 = sim.conservation()
+    assert abs(m1[0] - m0[0]) <= 1e-9 * m0[0]
+    assert abs(m1[1] - m0[1]) <= 1e-9 * m0[0] and abs(m1[2] - m0[2]) <= 1e-9 * m0[0]

@@ -183,3 +183,21 @@ def test_closure_projection_conserves_moments():
     # the transpose really is the adjoint
     g = np.random.default_rng(2).standard_normal((50, 9))
     assert abs((ref.project(v) * g).sum() - (v * ref.project_t(g)).sum()) < 1e-10
+
+
+def test_closure_stress_loss_gradient_against_finite_differences():
+    """The restatement of the stress target's loss: its gradient against central differences."""
+    from oracle import closure_ref as ref
+
+    rng = np.random.default_rng(0)
+    p = 0.05 * rng.standard_normal(9 * 9 * 32 + 32 + 9 * 32 * 32 + 32 + 9 * 32 * 9 + 9)
+    x0 = rng.standard_normal((1, 16, 16, 9))
+    T = 0.1 * rng.standard_normal((1, 16, 16, 9))
+    _, g = ref.stress_loss_and_grad(x0, T, p, 0.7, emulate_bf16=False)
+    for k in (5, 2600, 3000, 9000, 12000, 14468):
+        e = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[k] += e
+        pm[k] -= e
+        fd = (ref.stress_loss_and_grad(x0, T, pp, 0.7, False)[0] - ref.stress_loss_and_grad(x0, T, pm, 0.7, False)[0]) / (2 * e)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g[k])) + 1e-9, (k, fd, g[k])
