@@ -117,13 +117,16 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
         if (x < 0) { --y; x += dm.pitch; }
         if (x >= dm.pitch) { ++y; x -= dm.pitch; }
         if (y >= dm.ny || x >= dm.nx) return;  // past the domain's end, or a padding column
-        // pool base pointers and the domain's offsets (not per-domain pointers: fewer registers)
+        // pool base pointers and the domain's 32-bit offsets (not per-domain pointers: fewer
+        // registers; lbm_batch_create keeps the pools below 2^32 elements)
         if (write_macro)
-            phys_cell_update<StoreF32, true, LBM_COLLISION_BGK, false, size_t>(
-                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
+            phys_cell_update<StoreF32, true, LBM_COLLISION_BGK, false, uint32_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, (uint32_t)dm.pop_off,
+                (uint32_t)dm.cell_off);
         else
-            phys_cell_update<StoreF32, false, LBM_COLLISION_BGK, false, size_t>(
-                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
+            phys_cell_update<StoreF32, false, LBM_COLLISION_BGK, false, uint32_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, (uint32_t)dm.pop_off,
+                (uint32_t)dm.cell_off);
         return;
     }
     const int y = tl.z + (int)threadIdx.y;
@@ -132,11 +135,13 @@ __device__ __forceinline__ void tile_update(const BatchDomain* __restrict__ doms
         const int x = tl.y + (int)threadIdx.x;
         if (x >= dm.nx) return;
         if (write_macro)
-            phys_cell_update<StoreF32, true, LBM_COLLISION_BGK, false, size_t>(
-                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
+            phys_cell_update<StoreF32, true, LBM_COLLISION_BGK, false, uint32_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, (uint32_t)dm.pop_off,
+                (uint32_t)dm.cell_off);
         else
-            phys_cell_update<StoreF32, false, LBM_COLLISION_BGK, false, size_t>(
-                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, dm.pop_off, dm.cell_off);
+            phys_cell_update<StoreF32, false, LBM_COLLISION_BGK, false, uint32_t>(
+                A0, B0, flags, info, dm.omega, x, y, dm.nx, dm.pitch, dm.ny, macro, 0u, (uint32_t)dm.pop_off,
+                (uint32_t)dm.cell_off);
     } else {
         const int x0 = tl.y + (int)threadIdx.x * 4;
         const bool active = x0 < dm.nx;
@@ -553,6 +558,9 @@ int lbm_batch_create(int32_t n, const lbm_domain_desc* desc, lbm_batch** out) {
         live += (size_t)d.nx * d.ny;
     }
     if (cells > ((size_t)1 << 31)) return bfail(LBM_ERR_ARG, "batch of %zu cells exceeds 2^31", cells);
+    // the one-cell updates address the pools with 32-bit element offsets
+    if (pop >= ((size_t)1 << 32))
+        return bfail(LBM_ERR_ARG, "batch of %zu population elements reaches 2^32 (at most ~477 M padded cells)", pop);
     lbm_batch* b = new (std::nothrow) lbm_batch();
     if (!b) return bfail(LBM_ERR_NOMEM, "out of host memory");
     b->desc.assign(desc, desc + n);
