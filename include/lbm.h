@@ -171,9 +171,25 @@ int lbm_abi_version(void);
 const char* lbm_last_error(void);
 void lbm_params_default(lbm_params* p);
 
-/* lifetime -- FluidSimulator::new / drop */
+/* lifetime -- FluidSimulator::new / drop.  lbm_destroy waits for the lattice's stream; work
+   the caller queued on other streams that reads the lattice's buffers (lbm_device_populations,
+   lbm_device_macro) must be complete before it is called. */
 int lbm_create(const lbm_params* p, lbm_handle** out);
 int lbm_destroy(lbm_handle* h);
+
+/* Device memory of lattices.  lbm_create takes a lattice's buffers from a stream-ordered
+   memory pool of the current device that the library owns, and lbm_destroy returns them there.
+   The pool keeps up to `bytes` of returned memory reserved (default: an eighth of the device's
+   memory, at most 16 GiB), so a lattice created after another was destroyed is served without
+   a new device allocation.  lbm_memory_set_retain sets that limit for every device (0: give
+   memory back at each synchronisation); lbm_memory_trim waits for the current device and gives
+   its pool's unused memory back; lbm_memory_stats reads the current device pool's reserved and
+   used bytes (0 and 0 before its first lattice).  Like every cached device state of the
+   library, the pools belong to the device's primary context: a cudaDeviceReset invalidates
+   them.  No counterpart in the reference (wgpu owns its buffers). */
+int lbm_memory_set_retain(uint64_t bytes);
+int lbm_memory_trim(void);
+int lbm_memory_stats(uint64_t* reserved, uint64_t* used);
 /* run the handle's work on a caller-owned cudaStream_t (NULL restores its own stream);
    no counterpart in the reference */
 int lbm_set_stream(lbm_handle* h, void* cuda_stream);

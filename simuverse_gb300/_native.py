@@ -97,6 +97,9 @@ _D = ctypes.c_double
 
 # name -> argtypes; every function returns int
 _SIGNATURES = {
+    "lbm_memory_set_retain": [ctypes.c_uint64],
+    "lbm_memory_trim": [],
+    "lbm_memory_stats": [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
     "lbm_create": [ctypes.POINTER(LbmParams), ctypes.POINTER(_P)],
     "lbm_destroy": [_P],
     "lbm_set_stream": [_P, _P],

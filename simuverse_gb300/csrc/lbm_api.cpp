@@ -46,6 +46,62 @@ int fail(int code, const char* fmt, ...) {
         if (r_ < 0) return r_; \
     } while (0)
 
+// Lattice memory.  A lattice's device buffers come from one stream-ordered pool per device
+// that the library owns (cudaMallocFromPoolAsync on the lattice's stream).  lbm_destroy gives
+// them back with cudaFreeAsync, and the pool keeps up to `retain` bytes of returned memory
+// reserved, so the next lattice of a similar size is served from it without a device
+// allocation (cudaMalloc of the 1.7 GB of a 4096^2 FP32 lattice takes about 0.5 ms).
+std::mutex g_pool_mu;
+uint64_t g_retain = 0;       // bytes a pool keeps; 0 until set: the default of each device
+bool g_retain_set = false;
+lbm::PerDevice<cudaMemPool_t> g_pools;
+
+uint64_t default_retain(int dev) {
+    size_t total = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) total = prop.totalGlobalMem;
+    return std::min<uint64_t>((uint64_t)total / 8, (uint64_t)16 << 30);
+}
+
+cudaError_t device_pool(int dev, cudaMemPool_t* out) {
+    return g_pools.get(
+        dev,
+        [&](cudaMemPool_t& pool) {
+            cudaMemPoolProps props;
+            std::memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaError_t e = cudaMemPoolCreate(&pool, &props);
+            if (e != cudaSuccess) return e;
+            uint64_t keep;
+            {
+                std::lock_guard<std::mutex> lock(g_pool_mu);
+                keep = g_retain_set ? g_retain : default_retain(dev);
+            }
+            e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            if (e != cudaSuccess) cudaMemPoolDestroy(pool);
+            return e;
+        },
+        out);
+}
+
+// bytes of device memory on the current device, ordered on stream s
+template <class T>
+cudaError_t pool_alloc(T** p, size_t bytes, cudaStream_t s) {
+    *p = nullptr;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    cudaMemPool_t pool = nullptr;
+    if (e == cudaSuccess) e = device_pool(dev, &pool);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void**)p, bytes, pool, s);
+    return e;
+}
+
+void pool_free(void* p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+}
+
 constexpr float OBSTACLE_RADIUS = 28.0f;  // fluid/mod.rs:1
 
 bool sd_sphere(float px, float py, float r) {  // fluid/mod.rs:57-59 (glam Vec2::length)
@@ -127,14 +183,50 @@ void disk_cells(int nx, int ny, double cx, double cy, double r, F&& visit) {
         }
 }
 
+// Number of cells disk_cells visits, one row at a time.  On a row the test holds on one run of
+// x around cx: the rounded (x - cx)^2 does not decrease as |x - cx| grows, since rounding is
+// monotone.  So the run's ends are found from sqrt(r^2 - dy^2) and corrected by evaluating
+// the exact test, and the count equals the cell-by-cell loop's.
+long disk_cell_count(int nx, int ny, double cx, double cy, double r) {
+    const int bx0 = std::max((int)std::floor(cx - r), 1), bx1 = std::min((int)std::ceil(cx + r), nx - 2);
+    const int by0 = std::max((int)std::floor(cy - r), 1), by1 = std::min((int)std::ceil(cy + r), ny - 2);
+    const int xf = (int)std::floor(cx);  // the lattice points nearest cx are xf and xf + 1
+    long n = 0;
+    for (int y = by0; y <= by1; ++y) {
+        const double dy = (double)y - cy;
+        auto in = [&](int x) {
+            const double dx = (double)x - cx;
+            return dx * dx + dy * dy <= r * r;
+        };
+        // the run, if any, holds the row's point nearest cx
+        const int xm = in(xf) ? xf : xf + 1;
+        if (!in(xm)) continue;
+        const double w = std::sqrt(std::max(0.0, r * r - dy * dy));
+        int hi = std::max(xm, (int)std::floor(cx + w)), lo = std::min(xm, (int)std::ceil(cx - w));
+        if (in(hi)) { while (in(hi + 1)) ++hi; } else { while (!in(hi)) --hi; }
+        if (in(lo)) { while (in(lo - 1)) --lo; } else { while (!in(lo)) ++lo; }
+        lo = std::max(lo, bx0);
+        hi = std::min(hi, bx1);
+        if (hi >= lo) n += hi - lo + 1;
+    }
+    return n;
+}
+
 // The disk list (cx, cy, r per disk).  Accepted disks keep a gap of 2 cells, so no cell
 // belongs to two disks and every disk cell is a bulk cell of the base pattern: the solid
-// count is the sum of the disks' cell counts.
+// count is the sum of the disks' cell counts.  A candidate is tested only against the disks
+// in its own and the eight neighbouring squares of a grid whose side is at least the largest
+// centre distance that can overlap (2 rmax + 2); the test itself is the plain pairwise one, so
+// the accepted list, and the generator's draws, do not depend on the grid.
 std::vector<double> channel_disks(int nx, int ny, uint64_t seed, float frac, float rmin, float rmax) {
     const long target = (long)std::ceil((double)frac * (double)nx * (double)ny);
     const double xlo = nx / 16 > 2 ? (double)(nx / 16) : 2.0;
     const double xhi = (double)(nx - 1) - (nx / 8 > 2 ? (double)(nx / 8) : 2.0);
     const double ylo = 2.0, yhi = (double)(ny - 3);
+    const double side = std::max({2.0 * (double)rmax + 2.0, (double)nx / 128.0, (double)ny / 128.0, 1.0});
+    const int gx = (int)((double)nx / side) + 1, gy = (int)((double)ny / side) + 1;
+    std::vector<std::vector<int>> grid((size_t)gx * gy);
+    auto square = [&](double v, int n) { return std::min(std::max((int)std::floor(v / side), 0), n - 1); };
     std::mt19937_64 g(seed);
     std::vector<double> disks;
     long solid = 0, attempts = 0;
@@ -145,14 +237,18 @@ std::vector<double> channel_disks(int nx, int ny, uint64_t seed, float frac, flo
         if (xhi - xlo < 2.0 * r || yhi - ylo < 2.0 * r) continue;
         const double cx = xlo + r + (xhi - xlo - 2.0 * r) * u2;
         const double cy = ylo + r + (yhi - ylo - 2.0 * r) * u3;
+        const int sx = square(cx, gx), sy = square(cy, gy);
         bool ok = true;
-        for (size_t k = 0; k < disks.size(); k += 3) {
-            const double dx = cx - disks[k], dy = cy - disks[k + 1], md = r + disks[k + 2] + 2.0;
-            if (dx * dx + dy * dy < md * md) { ok = false; break; }
-        }
+        for (int qy = std::max(sy - 1, 0); ok && qy <= std::min(sy + 1, gy - 1); ++qy)
+            for (int qx = std::max(sx - 1, 0); ok && qx <= std::min(sx + 1, gx - 1); ++qx)
+                for (int k : grid[(size_t)qy * gx + qx]) {
+                    const double dx = cx - disks[3 * k], dy = cy - disks[3 * k + 1], md = r + disks[3 * k + 2] + 2.0;
+                    if (dx * dx + dy * dy < md * md) { ok = false; break; }
+                }
         if (!ok) continue;
+        grid[(size_t)sy * gx + sx].push_back((int)(disks.size() / 3));
         disks.push_back(cx); disks.push_back(cy); disks.push_back(r);
-        disk_cells(nx, ny, cx, cy, r, [&](size_t) { ++solid; });
+        solid += disk_cell_count(nx, ny, cx, cy, r);
     }
     return disks;
 }
@@ -281,7 +377,7 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "the four-cell kernel needs physics mode and nx %% 4 == 0");
     if (p.kernel == LBM_KERNEL_BULK && (p.mode != LBM_MODE_PHYSICS || p.nx % 8 != 0))
         return fail(LBM_ERR_ARG, "the bulk-copy kernel needs physics mode and nx %% 8 == 0");
-    if (p.scene == LBM_SCENE_CHANNEL && !(p.disk_rmin >= 0.0f && p.disk_rmax >= p.disk_rmin && p.solid_fraction >= 0.0f &&
+    if (p.scene == LBM_SCENE_CHANNEL && !(p.disk_rmin >= 0.0f && p.disk_rmax >= p.disk_rmin && std::isfinite(p.disk_rmax) && p.solid_fraction >= 0.0f &&
                                          p.solid_fraction < 0.5f))
         return fail(LBM_ERR_ARG, "channel disk parameters out of range");
     return LBM_OK;
@@ -309,12 +405,13 @@ int build_scene_on_device(lbm_handle* h) {
     double* d_disks = nullptr;
     const int nd = (int)(disks.size() / 3);
     if (nd > 0) {
-        LBM_CK(cudaMalloc((void**)&d_disks, disks.size() * sizeof(double)));
+        LBM_CK(pool_alloc(&d_disks, disks.size() * sizeof(double), h->stream));
         cudaError_t e = cudaMemcpyAsync(d_disks, disks.data(), disks.size() * sizeof(double), cudaMemcpyHostToDevice,
                                         h->stream);
         if (e == cudaSuccess) e = lbm::launch_build_scene(h, d_disks, nd, h->stream);
+        pool_free(d_disks, h->stream);  // ordered after the kernels that read it
+        // the host list is read by the copy: it must not go away before the copy ran
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        cudaFree(d_disks);
         if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "scene mask on the device: %s", cudaGetErrorString(e));
     } else {
         LBM_CK(lbm::launch_build_scene(h, nullptr, 0, h->stream));
@@ -359,18 +456,24 @@ int sync(lbm_handle* h) {
     return LBM_OK;
 }
 
+// the lattice's buffers back to the pool (ordered on the lattice's own stream: the caller has
+// waited for the stream the lattice ran on)
 void free_all(lbm_handle* h) {
-    cudaFree(h->buf[0]);
-    cudaFree(h->buf[1]);
-    cudaFree(h->d_flags);
-    cudaFree(h->d_info);
-    cudaFree(h->d_macro);
-    cudaFree(h->d_part);
-    cudaFree(h->d_count);
-    cudaFree(h->d_status);
-    cudaFree(h->d_host_info);
-    cudaFree(h->d_edits);
-    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    cudaStream_t s = h->own_stream;
+    pool_free(h->buf[0], s);
+    pool_free(h->buf[1], s);
+    pool_free(h->d_flags, s);
+    pool_free(h->d_info, s);
+    pool_free(h->d_macro, s);
+    pool_free(h->d_part, s);
+    pool_free(h->d_count, s);
+    pool_free(h->d_status, s);
+    pool_free(h->d_host_info, s);
+    pool_free(h->d_edits, s);
+    if (s) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
 }
 
 int check_handle(const lbm_handle* h) {
@@ -390,6 +493,45 @@ int set_error(int code, const char* msg) {
 extern "C" {
 
 int lbm_abi_version(void) { return LBM_ABI_VERSION; }
+
+int lbm_memory_set_retain(uint64_t bytes) {
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mu);
+        g_retain = bytes;
+        g_retain_set = true;
+    }
+    int n = 0;
+    LBM_CK(cudaGetDeviceCount(&n));
+    for (int d = 0; d < n && d < lbm::MAX_DEVICES; ++d) {
+        cudaMemPool_t pool = nullptr;
+        if (!g_pools.peek(d, &pool)) continue;  // created later with the new value
+        LBM_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &bytes));
+    }
+    return LBM_OK;
+}
+
+int lbm_memory_trim(void) {
+    int dev = 0;
+    LBM_CK(cudaGetDevice(&dev));
+    cudaMemPool_t pool = nullptr;
+    if (!g_pools.peek(dev, &pool)) return LBM_OK;
+    LBM_CK(cudaDeviceSynchronize());  // frees still in flight return their memory first
+    LBM_CK(cudaMemPoolTrimTo(pool, 0));
+    return LBM_OK;
+}
+
+int lbm_memory_stats(uint64_t* reserved, uint64_t* used) {
+    if (!reserved || !used) return fail(LBM_ERR_ARG, "null argument");
+    *reserved = 0;
+    *used = 0;
+    int dev = 0;
+    LBM_CK(cudaGetDevice(&dev));
+    cudaMemPool_t pool = nullptr;
+    if (!g_pools.peek(dev, &pool)) return LBM_OK;
+    LBM_CK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, reserved));
+    LBM_CK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, used));
+    return LBM_OK;
+}
 
 const char* lbm_last_error(void) { return g_err.c_str(); }
 
@@ -434,15 +576,16 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
     const size_t pop_bytes = 9 * h->N * lbm::dtype_size(p.dtype);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     h->stream = h->own_stream;
-    if (e == cudaSuccess) e = cudaMalloc(&h->buf[0], pop_bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&h->buf[1], pop_bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_flags, h->N * sizeof(uint16_t));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_info, h->N * sizeof(lbm_lattice_info));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_macro, 3 * h->N * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_part, (size_t)lbm::RED_BLOCKS * 6 * sizeof(double) + 64 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_count, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_status, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int));
+    const cudaStream_t s = h->own_stream;
+    if (e == cudaSuccess) e = pool_alloc(&h->buf[0], pop_bytes, s);
+    if (e == cudaSuccess) e = pool_alloc(&h->buf[1], pop_bytes, s);
+    if (e == cudaSuccess) e = pool_alloc(&h->d_flags, h->N * sizeof(uint16_t), s);
+    if (e == cudaSuccess) e = pool_alloc(&h->d_info, h->N * sizeof(lbm_lattice_info), s);
+    if (e == cudaSuccess) e = pool_alloc(&h->d_macro, 3 * h->N * sizeof(float), s);
+    if (e == cudaSuccess) e = pool_alloc(&h->d_part, (size_t)lbm::RED_BLOCKS * 6 * sizeof(double) + 64 * sizeof(double), s);
+    if (e == cudaSuccess) e = pool_alloc(&h->d_count, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = pool_alloc(&h->d_status, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_status, 0, sizeof(int), s);
     if (e != cudaSuccess) {
         free_all(h);
         delete h;
@@ -696,7 +839,7 @@ int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* ap
         forces.swap(last);
     }
     if (!h->host_mirror_valid && !obs.empty()) {
-        if (!h->d_host_info) LBM_CK(cudaMalloc((void**)&h->d_host_info, h->N * sizeof(lbm_lattice_info)));
+        if (!h->d_host_info) LBM_CK(pool_alloc(&h->d_host_info, h->N * sizeof(lbm_lattice_info), h->stream));
         LBM_CK(cudaMemcpyAsync(h->d_host_info, h->host_info.data(), h->N * sizeof(lbm_lattice_info),
                                cudaMemcpyHostToDevice, h->stream));
         h->host_mirror_valid = true;
@@ -704,12 +847,11 @@ int lbm_apply_edits(lbm_handle* h, const lbm_edit* edits, int32_t n, int32_t* ap
     const size_t bytes = obs.size() * sizeof(lbm::EditObstacle) + forces.size() * sizeof(lbm::EditForce);
     if (bytes > 0) {
         if (bytes > h->edits_cap) {
-            LBM_CK(cudaStreamSynchronize(h->stream));  // the old list may still be read
-            cudaFree(h->d_edits);
+            pool_free(h->d_edits, h->stream);  // after the kernels that read the old list
             h->d_edits = nullptr;
             h->edits_cap = 0;
             const size_t cap = std::max(bytes, (size_t)4096);
-            LBM_CK(cudaMalloc(&h->d_edits, cap));
+            LBM_CK(pool_alloc(&h->d_edits, cap, h->stream));
             h->edits_cap = cap;
         }
         std::vector<unsigned char> stage(bytes);
@@ -811,11 +953,11 @@ int lbm_read_macro_rgba16f(lbm_handle* h, uint16_t* rgba) {
     if (!rgba) return fail(LBM_ERR_ARG, "null output");
     LBM_TRY(use_device(h));
     uint16_t* d = nullptr;
-    LBM_CK(cudaMalloc((void**)&d, 4 * h->N * sizeof(uint16_t)));
+    LBM_CK(pool_alloc(&d, 4 * h->N * sizeof(uint16_t), h->stream));
     cudaError_t e = lbm::launch_macro_rgba16f(h, d, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, d, 4 * h->N * sizeof(uint16_t), cudaMemcpyDeviceToHost, h->stream);
+    pool_free(d, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(d);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "rgba16f read-back: %s", cudaGetErrorString(e));
     ++h->launches;
     return LBM_OK;
@@ -832,11 +974,11 @@ int lbm_read_populations(lbm_handle* h, void* dst, int32_t dd) {
         return sync(h);
     }
     void* tmp = nullptr;
-    LBM_CK(cudaMalloc(&tmp, bytes));
+    LBM_CK(pool_alloc(&tmp, bytes, h->stream));
     cudaError_t e = lbm::launch_to_absolute(h, h->buf[h->cur], tmp, dd, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, bytes, cudaMemcpyDeviceToHost, h->stream);
+    pool_free(tmp, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(tmp);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "population read-back: %s", cudaGetErrorString(e));
     ++h->launches;
     return LBM_OK;
@@ -849,11 +991,11 @@ int lbm_write_populations(lbm_handle* h, const void* src, int32_t sd) {
     LBM_TRY(use_device(h));
     const size_t bytes = 9 * h->N * lbm::dtype_size(sd);
     void* tmp = nullptr;
-    LBM_CK(cudaMalloc(&tmp, bytes));
+    LBM_CK(pool_alloc(&tmp, bytes, h->stream));
     cudaError_t e = cudaMemcpyAsync(tmp, src, bytes, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = lbm::launch_from_absolute(h, tmp, sd, h->buf[h->cur], h->stream);
+    pool_free(tmp, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(tmp);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "population upload: %s", cudaGetErrorString(e));
     ++h->launches;
     return LBM_OK;
@@ -865,7 +1007,7 @@ int lbm_init_equilibrium(lbm_handle* h, const float* rho, const float* ux, const
     LBM_TRY(use_device(h));
     float* d = nullptr;
     const size_t plane = h->N * sizeof(float);
-    LBM_CK(cudaMalloc((void**)&d, 3 * plane));
+    LBM_CK(pool_alloc(&d, 3 * plane, h->stream));
     const float* src[3] = {rho, ux, uy};
     const float* dp[3] = {nullptr, nullptr, nullptr};
     cudaError_t e = cudaSuccess;
@@ -875,8 +1017,8 @@ int lbm_init_equilibrium(lbm_handle* h, const float* rho, const float* ux, const
             dp[k] = d + k * h->N;
         }
     if (e == cudaSuccess) e = lbm::launch_phys_init(h, dp[0], dp[1], dp[2], h->stream);
+    pool_free(d, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(d);
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "equilibrium initialisation: %s", cudaGetErrorString(e));
     ++h->launches;
     h->cur = 0;

@@ -87,6 +87,14 @@ struct PerDevice {
         *out = val[dev];
         return cudaSuccess;
     }
+    // the device's value if it was set up, without setting it up
+    bool peek(int dev, T* out) {
+        if (dev < 0 || dev >= MAX_DEVICES) return false;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!ready[dev]) return false;
+        *out = val[dev];
+        return true;
+    }
 };
 
 // bounds-checked builds (LBM_BOUNDS_CHECK, see in_bounds in lbm_common.cuh): the number of

@@ -73,6 +73,24 @@ def scene_disks(nx: int, ny: int, **kw) -> np.ndarray:
     return out
 
 
+def memory_set_retain(nbytes: int):
+    """Bytes of device memory that destroyed lattices leave reserved in the library's pool of
+    every device, for the next lattices (lbm_memory_set_retain)."""
+    nat.check(nat.load().lbm_memory_set_retain(int(nbytes)))
+
+
+def memory_trim():
+    """Give the current device pool's unused memory back to the device (lbm_memory_trim)."""
+    nat.check(nat.load().lbm_memory_trim())
+
+
+def memory_stats() -> dict:
+    """Reserved and used bytes of the current device's lattice pool (lbm_memory_stats)."""
+    r, u = ctypes.c_uint64(), ctypes.c_uint64()
+    nat.check(nat.load().lbm_memory_stats(ctypes.byref(r), ctypes.byref(u)))
+    return {"reserved": r.value, "used": u.value}
+
+
 class FluidSimulator:
     def __init__(self, nx: int, ny: int, **kw):
         """An nx x ny lattice (lbm_create).  Keywords, all optional (make_params): mode

@@ -140,6 +140,27 @@ def test_physics_masks_match_oracle(native):
         assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("nx,ny,seed,frac,rmin,rmax", [
+    (4096, 4096, 1234, 0.05, 8.0, 32.0),  # the channel workload of the benchmark
+    (333, 257, 7, 0.2, 3.0, 3.0),         # equal radii, dense
+    (500, 90, 99, 0.3, 0.0, 2.5),         # radii below three cells, very dense
+    (257, 511, 5, 0.12, 4.25, 19.75),     # quarter-cell radii
+    (40, 30, 3, 0.1, 30.0, 60.0),         # no disk fits: an empty list
+])
+def test_channel_masks_match_oracle(native, nx, ny, seed, frac, rmin, rmax):
+    """The disk sampler (grid-pruned overlap test, row-span cell count) accepts exactly the
+    disks of the oracle's plain rejection sampler, so the masks are equal record for record."""
+    got = _mask(native, nx, ny, 1, 3, inlet_speed=0.05, seed=seed, solid_fraction=frac, disk_rmin=rmin,
+                disk_rmax=rmax)
+    ref, n = oracle.mask_physics_channel(nx, ny, 0.05, seed, frac, rmin, rmax)
+    assert np.array_equal(got, ref)
+    from simuverse_gb300.fluid import scene_disks
+
+    d = scene_disks(nx, ny, mode="physics", scene="channel", inlet_speed=0.05, seed=seed, solid_fraction=frac,
+                    disk_radius=(rmin, rmax))
+    assert len(d) == n
+
+
 def test_obstacle_disc_matches_oracle(native):
     from simuverse_gb300 import _native as nat
 
