@@ -267,42 +267,109 @@ __global__ void k_curl4(Field f, float* __restrict__ out) {
     *reinterpret_cast<float4*>(out + (size_t)y * f.nx + x0) = r;
 }
 
-// one canvas pixel (px, py) of the field colour map: uv at the pixel centre, as the
-// full-screen triangle of bufferless.vs.wgsl interpolates it; every plane is sampled with
-// linear filtering and clamp-to-edge addressing, with exact FP32 weights
-__global__ void k_colorize(Field f, const float* __restrict__ curl, int cw, int ch, int mode, float4* __restrict__ rgba) {
-    const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y;
-    if (px >= cw) return;
-    const float u = __fdiv_rn(add_rn((float)px, 0.5f), (float)cw), v = __fdiv_rn(add_rn((float)py, 0.5f), (float)ch);
-    // the four texels around (u, v), clamped to the edge, shared by every sampled plane
-    const float tx = sub_rn(mul_rn(u, (float)f.nx), 0.5f), ty = sub_rn(mul_rn(v, (float)f.ny), 0.5f);
-    const float fx0 = floorf(tx), fy0 = floorf(ty);
-    const float ax = sub_rn(tx, fx0), ay = sub_rn(ty, fy0), bx = sub_rn(1.0f, ax), by = sub_rn(1.0f, ay);
-    const int x0 = (int)fx0, y0 = (int)fy0;
-    const int xa = x0 < 0 ? 0 : (x0 > f.nx - 1 ? f.nx - 1 : x0), xb = x0 + 1 < 0 ? 0 : (x0 + 1 > f.nx - 1 ? f.nx - 1 : x0 + 1);
-    const int ya = y0 < 0 ? 0 : (y0 > f.ny - 1 ? f.ny - 1 : y0), yb = y0 + 1 < 0 ? 0 : (y0 + 1 > f.ny - 1 ? f.ny - 1 : y0 + 1);
-    const size_t i00 = (size_t)ya * f.nx + xa, i10 = (size_t)ya * f.nx + xb;
-    const size_t i01 = (size_t)yb * f.nx + xa, i11 = (size_t)yb * f.nx + xb;
-    auto lerp = [&](float a, float b, float c, float d) {
-        return add_rn(mul_rn(add_rn(mul_rn(a, bx), mul_rn(b, ax)), by), mul_rn(add_rn(mul_rn(c, bx), mul_rn(d, ax)), ay));
-    };
-    auto plane = [&](const float* p) {
-        return lerp(h16(__ldg(p + i00)), h16(__ldg(p + i10)), h16(__ldg(p + i01)), h16(__ldg(p + i11)));
-    };
-    float3 m = make_float3(0.0f, 0.0f, 0.0f);  // no step since initialisation: a zero field
-    if (!f.zero) m = make_float3(plane(f.ux), plane(f.uy), plane(f.rho));
-    float4 out;
-    if (mode == LBM_COLOR_CURL) {
-        const float cv = curl ? lerp(__ldg(curl + i00), __ldg(curl + i10), __ldg(curl + i01), __ldg(curl + i11)) : 0.0f;
-        const float speed = add_rn(fabsf(m.x), fabsf(m.y));
-        const float3 col = hsv2rgb(cv, add_rn(0.6f, mul_rn(speed, 1.4f)), add_rn(0.6f, mul_rn(m.z, 0.33f)));
-        out = make_float4(col.x, col.y, col.z, m.z);
-    } else {  // blend_img.wgsl: hue from atan2(ux, uy) with PI = 3.1415926
-        const float angle = __fdiv_rn(add_rn(atan2f(m.x, m.y), 3.1415926f), mul_rn(2.0f, 3.1415926f));
-        const float3 col = hsv2rgb(angle, 0.75f, 1.0f);
-        out = make_float4(col.x, col.y, col.z, 1.0f);
+// The field colour map: canvas pixel (px, py) samples each plane at uv = ((px + 0.5) / cw,
+// (py + 0.5) / ch), as the full-screen triangle of bufferless.vs.wgsl interpolates it, with
+// linear filtering and clamp-to-edge addressing and exact FP32 weights:
+//   h(row) = t[row][xa] bx + t[row][xb] ax,   value = h(ya) by + h(yb) ay
+// (every product and sum rounded on its own).  A thread owns one canvas column and COLOR_ROWS
+// consecutive pixels of it, so the column's weights and texel columns are computed once, and
+// the horizontal terms h of a texel row are kept while consecutive pixel rows sample it (a
+// canvas larger than the lattice samples each texel row for several pixel rows).  The rows'
+// weights are computed once per block.
+constexpr int COLOR_ROWS = 8;
+constexpr int COLOR_TPB = 128;
+
+template <int MODE>
+__global__ void __launch_bounds__(COLOR_TPB) k_colorize(Field f, const float* __restrict__ curl, int cw, int ch,
+                                                        float4* __restrict__ rgba) {
+    __shared__ float s_ay[COLOR_ROWS], s_by[COLOR_ROWS];
+    __shared__ int s_ya[COLOR_ROWS], s_yb[COLOR_ROWS];
+    const int py0 = blockIdx.y * COLOR_ROWS;
+    if (threadIdx.x < COLOR_ROWS) {
+        const int py = py0 + (int)threadIdx.x;
+        const float v = __fdiv_rn(add_rn((float)py, 0.5f), (float)ch);
+        const float ty = sub_rn(mul_rn(v, (float)f.ny), 0.5f);
+        const float fy0 = floorf(ty);
+        const float ay = sub_rn(ty, fy0);
+        const int y0 = (int)fy0;
+        s_ay[threadIdx.x] = ay;
+        s_by[threadIdx.x] = sub_rn(1.0f, ay);
+        s_ya[threadIdx.x] = y0 < 0 ? 0 : (y0 > f.ny - 1 ? f.ny - 1 : y0);
+        s_yb[threadIdx.x] = y0 + 1 < 0 ? 0 : (y0 + 1 > f.ny - 1 ? f.ny - 1 : y0 + 1);
     }
-    rgba[(size_t)py * cw + px] = out;
+    __syncthreads();
+    const int px = blockIdx.x * COLOR_TPB + threadIdx.x;
+    if (px >= cw) return;
+    const float u = __fdiv_rn(add_rn((float)px, 0.5f), (float)cw);
+    const float tx = sub_rn(mul_rn(u, (float)f.nx), 0.5f);
+    const float fx0 = floorf(tx);
+    const float ax = sub_rn(tx, fx0), bx = sub_rn(1.0f, ax);
+    const int x0 = (int)fx0;
+    const int xa = x0 < 0 ? 0 : (x0 > f.nx - 1 ? f.nx - 1 : x0), xb = x0 + 1 < 0 ? 0 : (x0 + 1 > f.nx - 1 ? f.nx - 1 : x0 + 1);
+    // horizontal terms of texel row y: ux, uy, rho (rounded to FP16 as macro_tex holds them), curl
+    constexpr int NP = MODE == LBM_COLOR_CURL ? 4 : 2;
+    auto row_terms = [&](int y, float* h) {
+        const size_t ra = (size_t)y * f.nx + xa, rb = (size_t)y * f.nx + xb;
+        const float* planes[3] = {f.ux, f.uy, f.rho};
+#pragma unroll
+        for (int k = 0; k < (NP < 3 ? NP : 3); ++k)
+            h[k] = f.zero ? 0.0f
+                          : add_rn(mul_rn(h16(__ldg(planes[k] + ra)), bx), mul_rn(h16(__ldg(planes[k] + rb)), ax));
+        if (NP == 4) h[3] = curl ? add_rn(mul_rn(__ldg(curl + ra), bx), mul_rn(__ldg(curl + rb), ax)) : 0.0f;
+    };
+    int r0 = -1, r1 = -1;  // texel rows whose terms h0, h1 hold
+    float h0[NP], h1[NP];
+#pragma unroll 1
+    for (int k = 0; k < COLOR_ROWS; ++k) {
+        const int py = py0 + k;
+        if (py >= ch) break;
+        const int ya = s_ya[k], yb = s_yb[k];
+        const float ay = s_ay[k], by = s_by[k];
+        float ha[NP], hb[NP];
+        // warp-uniform branches: every thread of the block is on the same pixel row
+        if (ya == r0) {
+#pragma unroll
+            for (int q = 0; q < NP; ++q) ha[q] = h0[q];
+        } else if (ya == r1) {
+#pragma unroll
+            for (int q = 0; q < NP; ++q) ha[q] = h1[q];
+        } else {
+            row_terms(ya, ha);
+        }
+        if (yb == ya) {
+#pragma unroll
+            for (int q = 0; q < NP; ++q) hb[q] = ha[q];
+        } else if (yb == r1) {
+#pragma unroll
+            for (int q = 0; q < NP; ++q) hb[q] = h1[q];
+        } else if (yb == r0) {
+#pragma unroll
+            for (int q = 0; q < NP; ++q) hb[q] = h0[q];
+        } else {
+            row_terms(yb, hb);
+        }
+        r0 = ya;
+        r1 = yb;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            h0[q] = ha[q];
+            h1[q] = hb[q];
+        }
+        float m[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) m[q] = add_rn(mul_rn(ha[q], by), mul_rn(hb[q], ay));
+        float4 out;
+        if (MODE == LBM_COLOR_CURL) {
+            const float speed = add_rn(fabsf(m[0]), fabsf(m[1]));
+            const float3 col = hsv2rgb(m[NP - 1], add_rn(0.6f, mul_rn(speed, 1.4f)), add_rn(0.6f, mul_rn(m[2 % NP], 0.33f)));
+            out = make_float4(col.x, col.y, col.z, m[2 % NP]);
+        } else {  // blend_img.wgsl: hue from atan2(ux, uy) with PI = 3.1415926
+            const float angle = __fdiv_rn(add_rn(atan2f(m[0], m[1]), 3.1415926f), mul_rn(2.0f, 3.1415926f));
+            const float3 col = hsv2rgb(angle, 0.75f, 1.0f);
+            out = make_float4(col.x, col.y, col.z, 1.0f);
+        }
+        rgba[(size_t)py * cw + px] = out;
+    }
 }
 
 }  // namespace view
@@ -603,9 +670,14 @@ int lbm_colorize(lbm_handle* h, int32_t mode, const float* d_curl, int32_t canva
     if (mode != LBM_COLOR_CURL && mode != LBM_COLOR_ANGLE) return vfail(LBM_ERR_ARG, "unknown colour mode %d", mode);
     if (canvas_w < 1 || canvas_h < 1 || canvas_h > 65535) return vfail(LBM_ERR_ARG, "canvas size out of range");
     V_CK(cudaSetDevice(h->device));
-    const dim3 grid((unsigned)((canvas_w + 127) / 128), (unsigned)canvas_h);
-    view::k_colorize<<<grid, 128, 0, h->stream>>>(field_of(h), d_curl, canvas_w, canvas_h, mode,
-                                                  reinterpret_cast<float4*>(d_rgba));
+    const dim3 grid((unsigned)((canvas_w + view::COLOR_TPB - 1) / view::COLOR_TPB),
+                    (unsigned)((canvas_h + view::COLOR_ROWS - 1) / view::COLOR_ROWS));
+    if (mode == LBM_COLOR_CURL)
+        view::k_colorize<LBM_COLOR_CURL><<<grid, view::COLOR_TPB, 0, h->stream>>>(
+            field_of(h), d_curl, canvas_w, canvas_h, reinterpret_cast<float4*>(d_rgba));
+    else
+        view::k_colorize<LBM_COLOR_ANGLE><<<grid, view::COLOR_TPB, 0, h->stream>>>(
+            field_of(h), d_curl, canvas_w, canvas_h, reinterpret_cast<float4*>(d_rgba));
     V_CK(cudaGetLastError());
     ++h->launches;
     return LBM_OK;

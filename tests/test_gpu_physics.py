@@ -80,6 +80,36 @@ def test_channel_fp32_parity(gpu):
     assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= 1e-4
 
 
+@pytest.mark.parametrize("scene,nx,ny", [("cavity", 65535, 5), ("cavity", 5, 65535), ("channel", 65535, 40),
+                                         ("channel", 40, 20000)])
+def test_extreme_aspect_parity(gpu, scene, nx, ny):
+    """The largest side the lattice takes (65535) as a row and as a column, a lattice whose rows
+    are longer than any block and one whose grid is all rows: 1 step at the 1e-5 bar, 60 steps
+    at the 1e-4 L2 bar."""
+    if scene == "cavity":
+        sim = FluidSimulator(nx, ny, mode="physics", scene="cavity", tau=0.6, lid_speed=0.1)
+        info = oracle.mask_physics_cavity(nx, ny, 0.1)
+        u_scale = 0.1
+    else:
+        sim = FluidSimulator(nx, ny, mode="physics", scene="channel", tau=0.56, inlet_speed=0.05, seed=5,
+                             solid_fraction=0.05, disk_radius=(3.0, 6.0))
+        info, _ = oracle.mask_physics_channel(nx, ny, 0.05, 5, 0.05, 3.0, 6.0)
+        u_scale = 0.05
+    assert np.array_equal(sim.info(), info)
+    ref = oracle.PhysOracle(info, sim.tau, np.float32)
+    sim.step(1)
+    ref.step(1)
+    e_rho, e_u = _macro_err(sim, ref, u_scale)
+    assert e_rho <= 1e-5 and e_u <= 1e-5
+    sim.step(59)
+    ref.step(59)
+    rho, ux, uy = sim.read_macro()
+    r_rho, r_ux, r_uy = ref.macro()
+    assert rel_l2(rho, r_rho) <= 1e-4
+    assert rel_l2(np.stack([ux, uy]), np.stack([r_ux, r_uy])) <= 1e-4
+    sim.close()
+
+
 def test_shear_wave_decay_matches_viscosity(gpu):
     """Periodic shear wave u_x = U sin(2 pi y / ny) decays as exp(-nu k^2 t), nu = (tau - 1/2)/3."""
     nx, ny, tau, U, steps = 64, 128, 0.8, 0.01, 2000

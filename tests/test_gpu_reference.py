@@ -138,7 +138,9 @@ def test_cavity_reset_keeps_host_mask(gpu):
 
 
 @pytest.mark.parametrize("scene,nx,ny", [("custom", 4, 4), ("custom", 5, 7), ("cavity", 129, 67),
-                                         ("poiseuille", 131, 97), ("cavity", 300, 5)])
+                                         ("poiseuille", 131, 97), ("cavity", 300, 5),
+                                         # the largest side the lattice takes, as a row and as a column
+                                         ("custom", 65535, 4), ("cavity", 6, 65535)])
 def test_odd_sizes(gpu, scene, nx, ny):
     sim = FluidSimulator(nx, ny, mode="reference", scene=scene, tau=0.57)
     ref = oracle.RefOracle(nx, ny, scene, tau=0.57)

@@ -105,11 +105,26 @@ def test_colorize_matches_oracle(gpu, mode):
     sim.step(60)
     rho, ux, uy = sim.read_macro()
     c = oracle.curl(ux, uy)
-    for cw, ch in ((sim.nx * 2, sim.ny * 2), (sim.nx * 3 + 1, sim.ny - 5)):
+    # 2x (the UI's canvas), enlarged and reduced ragged canvases (pixel rows that share texel rows,
+    # skip them, or fall in a partial block of 8 rows)
+    for cw, ch in ((sim.nx * 2, sim.ny * 2), (sim.nx * 3 + 1, sim.ny - 5), (sim.nx // 2 + 3, sim.ny * 5 + 3),
+                   (129, 7)):
         got = colorize(sim, mode, cw, ch)
         ref = oracle.colorize(rho, ux, uy, c if mode == "curl" else None, cw, ch, 0 if mode == "curl" else 1)
         assert got.shape == ref.shape
         assert np.max(np.abs(got - ref)) < 1e-5, np.max(np.abs(got - ref))
+    sim.close()
+
+
+def test_colorize_before_the_first_step(gpu):
+    """Before the first step macro_tex holds zeros: the colour map samples a zero field."""
+    sim = _sim("cavity")
+    rho, ux, uy = sim.read_macro()
+    c = curl(sim)
+    for mode in ("curl", "angle"):
+        got = colorize(sim, mode, 50, 30)
+        ref = oracle.colorize(rho, ux, uy, c if mode == "curl" else None, 50, 30, 0 if mode == "curl" else 1, zero=True)
+        assert np.max(np.abs(got - ref)) < 1e-5, (mode, np.max(np.abs(got - ref)))
     sim.close()
 
 
