@@ -101,6 +101,23 @@ def test_scene_disks_are_the_channel_obstacles(native):
     assert ras.sum() >= 0.06 * p.nx * p.ny
 
 
+def test_header_serves_a_c99_client(native, tmp_path):
+    """include/lbm.h is plain C99: the C client (tests/abi_client.c) compiles with warnings as
+    errors and links against liblbm.so alone (it runs on a GPU in tests/test_gpu_abi.py)."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    from test_gpu_abi import build_client
+
+    exe = build_client(tmp_path)
+    assert os.path.exists(exe)
+    out = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True).stdout
+    used = sorted(set(re.findall(r"\b(lbm_[a-z0-9_]+)", out)))
+    assert "lbm_create" in used and "lbm_read_macro" in used and "lbm_memory_stats" in used
+
+
 def test_null_handles_are_errors(native):
     from simuverse_gb300 import _native as nat
 
