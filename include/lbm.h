@@ -502,11 +502,13 @@ int lbm_closure_set_form(lbm_closure* c, int32_t inputs, int32_t target, int32_t
 /* the stress target's factor n / (2 k): window of a pair in coarse steps over twice the
    interval between applications (default 0.5: one application per step over one step) */
 int lbm_closure_set_stress_factor(lbm_closure* c, float factor);
-/* inference kernel of lbm_closure_apply / lbm_closure_predict: FUSED (default) computes the
+/* kernels of the closure.  FUSED (default): lbm_closure_apply / lbm_closure_predict compute the
    features and the three layers in one kernel on the tcgen05 tensor cores with the activations
-   in shared and tensor memory; LAYERS runs the feature kernel and one mma.sync kernel per
-   layer with the activations in device memory (the training path's kernels).  Both give the
-   same network within BF16 rounding of the activations. */
+   in shared and tensor memory, and training computes the weight gradients on the tcgen05 tensor
+   cores (crops a multiple of 64 wide; others on the CUDA cores).  LAYERS: the feature kernel and
+   one mma.sync kernel per layer with the activations in device memory, and the weight gradients
+   on the CUDA cores.  Both give the same network within BF16 rounding of the activations, and
+   the same gradients within FP32 summation order. */
 #define LBM_CLOSURE_KERNEL_FUSED 0
 #define LBM_CLOSURE_KERNEL_LAYERS 1
 int lbm_closure_set_kernel(lbm_closure* c, int32_t kernel);

@@ -67,8 +67,9 @@ class Closure:
     KERNELS = {"fused": 0, "layers": 1}
 
     def set_kernel(self, kernel: str = "fused"):
-        """Inference kernel of apply / predict: 'fused' (one tcgen05 kernel, activations on chip)
-        or 'layers' (feature kernel + one mma.sync kernel per layer)."""
+        """'fused': apply / predict as one tcgen05 kernel with the activations on chip, and the
+        training weight gradients on the tcgen05 tensor cores; 'layers': feature kernel + one
+        mma.sync kernel per layer, and the weight gradients on the CUDA cores."""
         nat.check(self._lib.lbm_closure_set_kernel(self._h, self.KERNELS[kernel]))
         self.kernel = kernel
 

@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <type_traits>
 #include <vector>
 
 #include "lbm_closure_kernels.cuh"
@@ -610,14 +611,38 @@ int forward(lbm_closure* c, const __nv_bfloat16* x0, __nv_bfloat16* x1, __nv_bfl
     return LBM_OK;
 }
 
+// weight and bias gradients of one layer: on the tcgen05 tensor cores (FUSED kernels, crops a
+// multiple of 64 wide), else on the CUDA cores; both write per-block partial sums that
+// k_dweight_final adds in block order
 template <int CIN, int COUT, class GT>
 int dweight(lbm_closure* c, const __nv_bfloat16* x, const GT* gr, int nimg, int H, int W, float* out) {
     constexpr int threads = 9 * (CIN / 4) * (COUT / 8);
     constexpr int len = 9 * CIN * COUT + COUT;
-    cl::k_dweight<CIN, COUT, GT, false><<<cl::DW_BLOCKS, threads, 0, c->stream>>>(x, gr, nimg, H, W, 0, H, 0, W,
-                                                                                   c->dwpart);
+    int blocks = cl::DW_BLOCKS;
+    if (std::is_same<GT, __nv_bfloat16>::value && c->kernel == LBM_CLOSURE_KERNEL_FUSED && W % cl::tc::DW_TILE == 0) {
+        using L = cl::tc::DwLayout<CIN, COUT>;
+        static lbm::PerDevice<int> sms;  // the attribute is set per device (c's device is current)
+        int nsm = 0;
+        C_CK(sms.get(
+            c->device,
+            [&](int& v) {
+                cudaError_t e = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, c->device);
+                if (e == cudaSuccess)
+                    e = cudaFuncSetAttribute(cl::tc::k_dweight_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             L::SMEM);
+                return e;
+            },
+            &nsm));
+        const int ntiles = nimg * H * (W / cl::tc::DW_TILE);
+        blocks = std::min(std::min(nsm, cl::DW_BLOCKS), ntiles);
+        cl::tc::k_dweight_tc<CIN, COUT><<<blocks, cl::tc::DW_THREADS, L::SMEM, c->stream>>>(
+            x, reinterpret_cast<const __nv_bfloat16*>(gr), nimg, H, W, c->dwpart, c->d_status);
+    } else {
+        cl::k_dweight<CIN, COUT, GT, false><<<cl::DW_BLOCKS, threads, 0, c->stream>>>(x, gr, nimg, H, W, 0, H, 0, W,
+                                                                                       c->dwpart);
+    }
     C_CK(cudaGetLastError());
-    cl::k_dweight_final<<<(len + 255) / 256, 256, 0, c->stream>>>(c->dwpart, cl::DW_BLOCKS, len, 1.0f, out);
+    cl::k_dweight_final<<<(len + 255) / 256, 256, 0, c->stream>>>(c->dwpart, blocks, len, 1.0f, out);
     C_CK(cudaGetLastError());
     c->launches += 2;
     return LBM_OK;

@@ -422,4 +422,215 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// Weight gradients of one layer on the tensor cores (training):
+//   dW[tap][ci][co] = sum_cells x[cell + off(tap)][ci] g[cell][co],   db[co] = sum_cells g[cell][co]
+// over every cell of nimg images of H x W (W % 64 == 0; inputs outside an image read as zero),
+// as one GEMM per CTA with the cells as the K dimension: A = the 9 shifted input windows stacked
+// along M (row tap * CIN + ci, plus a row of ones whose product is db, zero rows up to a multiple
+// of 128), B = the output gradients (N = COUT), D in tensor memory, accumulated over all the
+// CTA's tiles.  A tile is 64 cells of one image row (K = 64: 4 MMAs of K16 per M tile).
+//
+// Staging.  The tile's 3 input rows (66 cells each, x0 - 1 .. x0 + 64) and its 64 gradient cells
+// are copied as they are stored (NHWC, channels contiguous) into shared memory with cp.async;
+// ldmatrix.trans then turns each 8-cell x 8-channel block into the canonical K-major core matrix
+// (8 rows = channels, 16 bytes = 8 cells): thread t of the warp receives exactly the 4 bytes at
+// offset 4t of the core matrix, so the stores are contiguous.  Operand layout [k chunk][row][8]:
+// the descriptor's leading (K) offset is rows * 16, its stride (8-row) offset 128, as in the
+// inference kernel.  Raw tiles and operands are double-buffered: the copy of tile i + 1 and the
+// transposes of tile i overlap the MMAs of tile i - 1; before operand buffer b is rewritten,
+// thread 0 waits (1 s limit) for the commit of the MMAs that read it.  Each CTA writes its
+// partial sums in the CUDA-core kernel's layout, so k_dweight_final reduces them the same way.
+constexpr int DW_TILE = 64;
+constexpr int DW_THREADS = 256;
+constexpr int DW_TMEM_COLS = 128;
+
+template <int CIN, int COUT>
+struct DwLayout {
+    static constexpr int MROWS = 9 * CIN + 1;  // shifted inputs and the ones row
+    static constexpr int MT = (MROWS + 127) / 128;
+    static constexpr int MTOT = MT * 128;
+    static constexpr int XSTR = CIN * 2 + 16;  // padded: ldmatrix rows 8 cells apart hit distinct banks
+    static constexpr int GSTR = COUT * 2 + 16;
+    static constexpr int RAW_X = 3 * (DW_TILE + 2) * XSTR;
+    static constexpr int RAW = ((RAW_X + DW_TILE * GSTR + 127) / 128) * 128;
+    static constexpr int A_BYTES = MTOT * DW_TILE * 2;
+    static constexpr int B_BYTES = COUT * DW_TILE * 2;
+    static constexpr int OFF_A = 2 * RAW;
+    static constexpr int OFF_B = OFF_A + 2 * A_BYTES;
+    static constexpr int OFF_BAR = OFF_B + 2 * B_BYTES;
+    static constexpr int OFF_TSLOT = OFF_BAR + 16;
+    static constexpr int SMEM = OFF_TSLOT + 16;
+    static_assert(MT * COUT <= DW_TMEM_COLS, "accumulators fit the allocation");
+    static_assert(OFF_A % 128 == 0 && OFF_B % 128 == 0 && OFF_BAR % 8 == 0, "alignment");
+    static_assert(SMEM <= 227 * 1024, "one CTA per SM");
+};
+
+__device__ __forceinline__ void ldsm_x4_trans(unsigned (&r)[4], unsigned addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr));
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(DW_THREADS, 1)
+    k_dweight_tc(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ g, int nimg, int H, int W,
+                 float* __restrict__ partials, int* __restrict__ status) {
+    using L = DwLayout<CIN, COUT>;
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned bar0 = su32(sm + L::OFF_BAR);  // one mbarrier per operand buffer, 8 bytes apart
+    unsigned* tslot = reinterpret_cast<unsigned*>(sm + L::OFF_TSLOT);
+    const int tiles_x = W / DW_TILE, tiles_img = H * tiles_x, ntiles = nimg * tiles_img;
+
+    // rows of A that no tile writes: the ones row (db) and the zero rows, in both buffers
+    for (int i = tid; i < 2 * 8 * (L::MTOT - 9 * CIN); i += DW_THREADS) {
+        const int b = i / (8 * (L::MTOT - 9 * CIN)), rem = i % (8 * (L::MTOT - 9 * CIN));
+        const int kc = rem / (L::MTOT - 9 * CIN), m = 9 * CIN + rem % (L::MTOT - 9 * CIN);
+        const unsigned v = m == 9 * CIN ? 0x3F803F80u : 0u;  // BF16 1.0 pairs
+        *reinterpret_cast<uint4*>(sm + L::OFF_A + b * L::A_BYTES + (kc * L::MTOT + m) * 16) = make_uint4(v, v, v, v);
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                     "r"(DW_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+
+    // raw copies of tile t into raw buffer b: 3 input rows of 66 cells and 64 gradient cells
+    auto stage = [&](int t, int b) {
+        const int img = t / tiles_img, rem = t % tiles_img, y = rem / tiles_x, x0 = (rem % tiles_x) * DW_TILE;
+        unsigned char* rx = sm + b * L::RAW;
+        unsigned char* rg = rx + L::RAW_X;
+        constexpr int XC = CIN / 8, GC = COUT / 8;
+        for (int i = tid; i < 3 * (DW_TILE + 2) * XC; i += DW_THREADS) {
+            const int cc = i % XC, col = (i / XC) % (DW_TILE + 2), r = i / (XC * (DW_TILE + 2));
+            const int gy = y + r - 1, gx = x0 + col - 1;
+            const bool in = gy >= 0 && gy < H && gx >= 0 && gx < W;
+            const __nv_bfloat16* src = in ? x + ((((size_t)img * H + gy) * W + gx) * CIN + cc * 8) : x;
+            cp_async16(reinterpret_cast<unsigned*>(rx + (r * (DW_TILE + 2) + col) * L::XSTR + cc * 16), src, in);
+        }
+        for (int i = tid; i < DW_TILE * GC; i += DW_THREADS) {
+            const int cc = i % GC, cell = i / GC;
+            cp_async16(reinterpret_cast<unsigned*>(rg + cell * L::GSTR + cc * 16),
+                       g + ((((size_t)img * H + y) * W + x0 + cell) * COUT + cc * 8), true);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    // operands of raw buffer b into operand buffer b: A (9 CIN rows) and B (COUT rows), K = 64
+    auto transpose = [&](int b) {
+        const unsigned rx = su32(sm + b * L::RAW), rg = rx + L::RAW_X;
+        unsigned char* A = sm + L::OFF_A + b * L::A_BYTES;
+        unsigned char* Bm = sm + L::OFF_B + b * L::B_BYTES;
+        constexpr int JA = 9 * (CIN / 8) * 8, JB = (COUT / 8) * 8;  // core matrices (multiples of 4)
+        for (int u = warp; u < (JA + JB) / 4; u += DW_THREADS / 32) {
+            const int job = 4 * u + (lane >> 3), j = lane & 7;  // this thread's row address
+            unsigned addr;
+            if (job < JA) {
+                const int kc = job % 8, cg = (job / 8) % (CIN / 8), tap = job / (8 * (CIN / 8));
+                const int dy = tap / 3, dx = tap % 3;  // raw row dy holds image row y + dy - 1
+                addr = rx + (unsigned)((dy * (DW_TILE + 2) + kc * 8 + j + dx) * L::XSTR + cg * 16);
+            } else {
+                const int q = job - JA, kc = q % 8, ng = q / 8;
+                addr = rg + (unsigned)((kc * 8 + j) * L::GSTR + ng * 16);
+            }
+            unsigned r[4];
+            ldsm_x4_trans(r, addr);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+                const int jb = 4 * u + q4;
+                unsigned char* dst;
+                if (jb < JA) {
+                    const int kc = jb % 8, cg = (jb / 8) % (CIN / 8), tap = jb / (8 * (CIN / 8));
+                    dst = A + (kc * L::MTOT + tap * CIN + cg * 8) * 16;
+                } else {
+                    const int q = jb - JA, kc = q % 8, ng = q / 8;
+                    dst = Bm + (kc * COUT + ng * 8) * 16;
+                }
+                *reinterpret_cast<unsigned*>(dst + 4 * lane) = r[q4];
+            }
+        }
+    };
+
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tmem = *tslot;
+    constexpr uint32_t ID = idesc_bf16(128, COUT);
+    bool alive = true;
+    int i = 0, last = -1;
+    if ((int)blockIdx.x < ntiles) stage(blockIdx.x, 0);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+        const int b = i & 1;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        if (tid == 0) s_ok = i < 2 || bar_wait_bounded(bar0 + 8 * b, ((i - 2) >> 1) & 1) ? 1 : 0;
+        __syncthreads();
+        if (!s_ok) {
+            alive = false;
+            break;
+        }
+        transpose(b);
+        if (t + (int)gridDim.x < ntiles) stage(t + (int)gridDim.x, b ^ 1);
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            const unsigned a0 = su32(sm + L::OFF_A + b * L::A_BYTES), b0 = su32(sm + L::OFF_B + b * L::B_BYTES);
+#pragma unroll
+            for (int mt = 0; mt < L::MT; ++mt)
+#pragma unroll
+                for (int ks = 0; ks < DW_TILE / 16; ++ks) {
+                    const uint64_t ad = sdesc(a0 + (unsigned)((2 * ks * L::MTOT + mt * 128) * 16), L::MTOT * 16, 128);
+                    const uint64_t bd = sdesc(b0 + (unsigned)(2 * ks * COUT * 16), COUT * 16, 128);
+                    mma(tmem + (unsigned)(mt * COUT), ad, bd, ID, (i > 0 || ks > 0) ? 1u : 0u);
+                }
+            commit(bar0 + 8 * b);
+        }
+        last = i;
+    }
+    // the last commit covers every MMA of the CTA
+    if (tid == 0) s_ok = (last < 0 || bar_wait_bounded(bar0 + 8 * (last & 1), (last >> 1) & 1)) ? 1 : 0;
+    __syncthreads();
+    if (!s_ok) alive = false;
+    if (alive && last >= 0) {
+        fence_after();
+        const int lane_q = warp & 3, half = warp >> 2;
+        float* p = partials + (size_t)blockIdx.x * (9 * CIN * COUT + COUT);
+        for (int mt = half; mt < L::MT; mt += 2) {
+            const int m = mt * 128 + lane_q * 32 + lane;
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((unsigned)(lane_q * 32) << 16) + (unsigned)(mt * COUT + c0), v);
+                float* o = m < 9 * CIN ? p + (size_t)m * COUT + c0 : (m == 9 * CIN ? p + 9 * CIN * COUT + c0 : nullptr);
+                if (o != nullptr)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) o[j] = v[j];
+            }
+        }
+    }
+    if (!alive) {  // a wait ran out: record it and let the MMAs in flight finish before freeing
+        if (tid == 0) {
+            atomicExch(status, LBM_ERR_TIMEOUT);
+            if (last >= 0) bar_wait_bounded(bar0 + 8 * (last & 1), (last >> 1) & 1);
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DW_TMEM_COLS)
+                     : "memory");
+    }
+}
+
 }  // namespace tc

@@ -106,14 +106,15 @@ def test_targets_match_restatement(gpu, target, projection):
     assert abs(got - expect) <= 1e-3 * expect, (got, expect)
 
 
-@pytest.mark.parametrize("projection", ["cell", "domain"])
-def test_gradients_match_fp64_restatement(gpu, projection):
+@pytest.mark.parametrize("projection,crop", [("cell", 32), ("domain", 32), ("cell", 64)])
+def test_gradients_match_fp64_restatement(gpu, projection, crop):
+    """crop 32: weight gradients on the CUDA cores; crop 64: on the tcgen05 tensor cores."""
     rng = np.random.default_rng(1)
     c = Closure(64, 64, seed=2, projection=projection)
     c.params = _random_params(c, rng)
-    c.reserve(4, 32, 2)
-    feats = rng.standard_normal((2, 32, 32, 9))
-    targets = 0.3 * rng.standard_normal((2, 32, 32, 9))
+    c.reserve(4, crop, 2)
+    feats = rng.standard_normal((2, crop, crop, 9))
+    targets = 0.3 * rng.standard_normal((2, crop, crop, 9))
     loss, g = c.loss_grad(feats, targets)
     loss_ref, g_ref = ref.loss_and_grad(feats, targets, c.params, emulate_bf16=True, project_cell=projection == "cell")
     assert abs(loss - loss_ref) / loss_ref < 1e-2
@@ -125,6 +126,36 @@ def test_gradients_match_fp64_restatement(gpu, projection):
         rel = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
         cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
         assert rel < 5e-2 and cos > 0.998, (n, rel, cos)
+
+
+@pytest.mark.parametrize("target", ["populations", "stress"])
+@pytest.mark.parametrize("crop", [64, 128])
+def test_tensor_core_weight_gradients_match_cuda_core_ones(gpu, target, crop):
+    """The training step's weight and bias gradients from the tcgen05 kernel (crops a multiple of
+    64 wide) equal the CUDA-core kernel's up to FP32 summation order, for every layer: both sum
+    the same BF16 products."""
+    rng = np.random.default_rng(7)
+    c = Closure(128, 128, seed=3, inputs="eq", target=target, projection="cell")
+    c.params = _random_params(c, rng)
+    c.reserve(4, crop, 3)
+    feats = rng.standard_normal((3, crop, crop, 9))
+    targets = 0.3 * rng.standard_normal((3, crop, crop, 9))
+    c.set_kernel("layers")
+    loss_a, g_a = c.loss_grad(feats, targets)
+    c.set_kernel("fused")
+    loss_b, g_b = c.loss_grad(feats, targets)
+    c.status()
+    assert loss_a == loss_b  # same forward kernels for training
+    off, prev = 0, 0.0
+    for n in (9 * 9 * 32, 32, 9 * 32 * 32, 32, 9 * 32 * 9, 9):
+        a, b = g_a[off:off + n].astype(np.float64), g_b[off:off + n].astype(np.float64)
+        off += n
+        # a bias block is measured against its layer's weight block too: the stress loss does not
+        # depend on the last bias, whose gradient is rounding noise
+        scale = max(np.linalg.norm(a), prev if n in (32, 9) else 0.0)
+        assert np.linalg.norm(a - b) <= 1e-5 * scale, (n, np.linalg.norm(a - b), scale)
+        prev = np.linalg.norm(a)
+    c.close()
 
 
 @pytest.mark.parametrize("form", FORMS, ids=["-".join(f) for f in FORMS])
