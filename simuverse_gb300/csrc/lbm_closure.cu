@@ -330,8 +330,9 @@ __global__ void k_loss(const float* __restrict__ y, const __nv_bfloat16* __restr
 // model is m(x) = -factor sum_i e_i P(y)_i(x - e_i) in output units, factor = n / (2 k).
 // Pass 1: over the cells [4, H-4) x [4, W-4) of every image the residual r = m - T_j, T_j =
 // sum_i e_i T_i the stored momentum target, into res (zero elsewhere), FP64 loss partials.
-__global__ void k_stress_residual(const float* __restrict__ y, const __nv_bfloat16* __restrict__ T, int nimg, int H,
+__global__ void k_stress_residual(const float* __restrict__ z, const __nv_bfloat16* __restrict__ T, int nimg, int H,
                                   int W, float factor, float2* __restrict__ res, double* __restrict__ part) {
+    // z: P(y) of every cell as 9 planes (k_project_planes), so each cell is projected once
     __shared__ double red[32];
     const size_t total = (size_t)nimg * H * W;
     double acc = 0.0;
@@ -345,12 +346,9 @@ __global__ void k_stress_residual(const float* __restrict__ y, const __nv_bfloat
 #pragma unroll
         for (int i = 1; i < 9; ++i) {  // P(y) of the source cell x - e_i, its population i
             const long src = (long)c - (long)EY(i) * W - EX(i);
-            float v[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) v[k] = y[(size_t)src * 16 + k];
-            project9(v);
-            mx += (float)EX(i) * v[i];
-            my += (float)EY(i) * v[i];
+            const float v = z[(size_t)i * total + (size_t)src];
+            mx += (float)EX(i) * v;
+            my += (float)EY(i) * v;
         }
         float tx = 0.0f, ty = 0.0f;
 #pragma unroll
@@ -398,11 +396,19 @@ __global__ void k_stress_grad(const float2* __restrict__ res, int nimg, int H, i
     }
 }
 
-__global__ void k_sum_partials(const double* __restrict__ part, int n, double scale, double* __restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) s += part[i];
-    out[0] = s * scale;
+__global__ void __launch_bounds__(256) k_sum_partials(const double* __restrict__ part, int n, double scale,
+                                                      double* __restrict__ out) {
+    // 256 threads: strided partial sums, then a fixed tree (deterministic)
+    __shared__ double s[256];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) a += part[i];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = s[0] * scale;
 }
 
 // coarse cell = block average of factor x factor fine cells: rho and momentum averaged,
@@ -504,6 +510,7 @@ struct lbm_closure {
     int kernel = LBM_CLOSURE_KERNEL_FUSED;  // inference: one tcgen05 kernel, or the three layer kernels
     float stress_factor = 0.5f;             // stress target: window / (2 x application interval)
     float* bres = nullptr;                  // stress target: residuals of a batch (2 floats per cell)
+    float* bz = nullptr;                    // stress target: P(y) of a batch (9 planes)
     float* zp = nullptr;                    // stress target: P(y) of the field, 9 planes
     int* d_status = nullptr;                // LBM_ERR_TIMEOUT from a bounded wait of the fused kernel
     double* dmeans = nullptr;  // reduction partials (RED_BLOCKS x 3) and the 3 field means
@@ -642,7 +649,7 @@ int dweight(lbm_closure* c, const __nv_bfloat16* x, const GT* gr, int nimg, int 
                                                                                        c->dwpart);
     }
     C_CK(cudaGetLastError());
-    cl::k_dweight_final<<<(len + 255) / 256, 256, 0, c->stream>>>(c->dwpart, blocks, len, 1.0f, out);
+    cl::k_dweight_final<<<(len + 31) / 32, 256, 0, c->stream>>>(c->dwpart, blocks, len, 1.0f, out);
     C_CK(cudaGetLastError());
     c->launches += 2;
     return LBM_OK;
@@ -654,22 +661,25 @@ int batch_loss(lbm_closure* c, int nimg) {
     const int S = c->crop;
     if (c->target == LBM_CLOSURE_TARGET_STRESS) {
         const double count = (double)nimg * (S - 8) * (S - 8) * 2.0;
-        cl::k_stress_residual<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, nimg, S, S, c->stress_factor,
+        const size_t cells = (size_t)nimg * S * S;
+        cl::k_project_planes<<<(unsigned)((cells + 255) / 256), 256, 0, c->stream>>>(c->by, cells, c->bz);
+        C_CK(cudaGetLastError());
+        cl::k_stress_residual<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->bz, c->bt, nimg, S, S, c->stress_factor,
                                                                         reinterpret_cast<float2*>(c->bres), c->lpart);
         C_CK(cudaGetLastError());
         cl::k_stress_grad<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(reinterpret_cast<const float2*>(c->bres), nimg, S, S,
                                                                     c->stress_factor, (float)(1.0 / count), c->bg3);
         C_CK(cudaGetLastError());
-        cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
+        cl::k_sum_partials<<<1, 256, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
         C_CK(cudaGetLastError());
-        c->launches += 3;
+        c->launches += 4;
         return LBM_OK;
     }
     const double count = (double)nimg * (S - 6) * (S - 6) * 9.0;
     cl::k_loss<<<lbm::RED_BLOCKS, 256, 0, c->stream>>>(c->by, c->bt, nimg, S, S, (float)(1.0 / count),
                                                          c->projection == LBM_CLOSURE_PROJECT_CELL, c->bg3, c->lpart);
     C_CK(cudaGetLastError());
-    cl::k_sum_partials<<<1, 32, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
+    cl::k_sum_partials<<<1, 256, 0, c->stream>>>(c->lpart, lbm::RED_BLOCKS, 1.0 / count, c->dloss);
     C_CK(cudaGetLastError());
     c->launches += 2;
     return LBM_OK;
@@ -785,7 +795,7 @@ int lbm_closure_destroy(lbm_closure* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->p,  c->g,  c->m,   c->v,   c->mask, c->wf1, c->wf2, c->wf3, c->wb3, c->wb2, c->x0,
                     c->x1, c->x2, c->y,   c->dsx, c->dst,  c->bx0, c->bt,  c->bx1, c->bx2, c->bg3, c->bg2,
-                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans, c->d_status, c->bres, c->zp};
+                    c->bg1, c->by, c->dwpart, c->lpart, c->dloss, c->dmeans, c->d_status, c->bres, c->bz, c->zp};
     for (void* b : bufs) cudaFree(b);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1004,6 +1014,8 @@ int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t
     c->by = nullptr;
     cudaFree(c->bres);
     c->bres = nullptr;
+    cudaFree(c->bz);
+    c->bz = nullptr;
     const size_t cs = (size_t)crop * crop;
     C_CK(dalloc(&c->dsx, (size_t)max_pairs * cs * 16));
     C_CK(dalloc(&c->dst, (size_t)max_pairs * cs * 16));
@@ -1016,6 +1028,7 @@ int lbm_closure_reserve(lbm_closure* c, int32_t max_pairs, int32_t crop, int32_t
     C_CK(dalloc(&c->bg1, (size_t)batch * cs * 32));
     C_CK(dalloc(&c->by, (size_t)batch * cs * 16));
     C_CK(dalloc(&c->bres, (size_t)batch * cs * 2));
+    C_CK(dalloc(&c->bz, (size_t)batch * cs * 9));
     c->cap = max_pairs;
     c->crop = crop;
     c->batch = batch;

@@ -272,14 +272,27 @@ __global__ void k_dweight(const __nv_bfloat16* __restrict__ x, const GT* __restr
         for (int j = 0; j < 8; ++j) p[9 * CIN * COUT + ob * 8 + j] = bacc[j];
 }
 
-// out[k] = scale * sum_b partials[b][k] in block order (deterministic)
-__global__ void k_dweight_final(const float* __restrict__ partials, int nblocks, int len, float scale,
-                                float* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= len) return;
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += (double)partials[(size_t)b * len + k];
-    out[k] = (float)(s * (double)scale);
+// out[k] = scale * sum_b partials[b][k]: 8 threads per output each add a fixed range of the
+// blocks in order, then the 8 sums are added in order (deterministic).  256 threads, 32 outputs
+// per block.
+__global__ void __launch_bounds__(256) k_dweight_final(const float* __restrict__ partials, int nblocks, int len,
+                                                       float scale, float* __restrict__ out) {
+    __shared__ double s[8][32];
+    const int kk = threadIdx.x & 31, seg = threadIdx.x >> 5;
+    const int k = blockIdx.x * 32 + kk;
+    double a = 0.0;
+    if (k < len) {
+        const int per = (nblocks + 7) / 8, b0 = seg * per, b1 = min(nblocks, b0 + per);
+        for (int b = b0; b < b1; ++b) a += (double)partials[(size_t)b * len + k];
+    }
+    s[seg][kk] = a;
+    __syncthreads();
+    if (seg == 0 && k < len) {
+        double t = 0.0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) t += s[j][kk];
+        out[k] = (float)(t * (double)scale);
+    }
 }
 
 }  // namespace closure

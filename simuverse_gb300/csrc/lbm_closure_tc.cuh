@@ -437,10 +437,12 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 // (8 rows = channels, 16 bytes = 8 cells): thread t of the warp receives exactly the 4 bytes at
 // offset 4t of the core matrix, so the stores are contiguous.  Operand layout [k chunk][row][8]:
 // the descriptor's leading (K) offset is rows * 16, its stride (8-row) offset 128, as in the
-// inference kernel.  Raw tiles and operands are double-buffered: the copy of tile i + 1 and the
+// inference kernel.  Raw tiles go through a ring of three buffers (the copies of the next two
+// tiles are in flight while a tile is transposed) and the operands are double-buffered: the
 // transposes of tile i overlap the MMAs of tile i - 1; before operand buffer b is rewritten,
-// thread 0 waits (1 s limit) for the commit of the MMAs that read it.  Each CTA writes its
-// partial sums in the CUDA-core kernel's layout, so k_dweight_final reduces them the same way.
+// thread 0 waits (1 s limit) for the commit of the MMAs that read it.  The address arithmetic
+// that does not depend on the tile is done once.  Each CTA writes its partial sums in the
+// CUDA-core kernel's layout, so k_dweight_final reduces them the same way.
 constexpr int DW_TILE = 64;
 constexpr int DW_THREADS = 256;
 constexpr int DW_TMEM_COLS = 128;
@@ -456,7 +458,8 @@ struct DwLayout {
     static constexpr int RAW = ((RAW_X + DW_TILE * GSTR + 127) / 128) * 128;
     static constexpr int A_BYTES = MTOT * DW_TILE * 2;
     static constexpr int B_BYTES = COUT * DW_TILE * 2;
-    static constexpr int OFF_A = 2 * RAW;
+    static constexpr int NRAW = 3;  // raw ring depth
+    static constexpr int OFF_A = NRAW * RAW;
     static constexpr int OFF_B = OFF_A + 2 * A_BYTES;
     static constexpr int OFF_BAR = OFF_B + 2 * B_BYTES;
     static constexpr int OFF_TSLOT = OFF_BAR + 16;
@@ -503,58 +506,82 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
 
-    // raw copies of tile t into raw buffer b: 3 input rows of 66 cells and 64 gradient cells
+    // raw copies of tile t into raw buffer b: 3 input rows of 66 cells and 64 gradient cells.
+    // Thread tid copies the 16-byte chunks tid, tid + 256, ... of the tile, the same in every tile.
+    constexpr int XC = CIN / 8, GC = COUT / 8;
+    constexpr int NXCH = 3 * (DW_TILE + 2) * XC, NGCH = DW_TILE * GC;
+    constexpr int NCOPY = (NXCH + NGCH + DW_THREADS - 1) / DW_THREADS;
+    int crow[NCOPY], ccol[NCOPY];  // input chunk: raw row, column (-1: a gradient chunk; -2: none)
+    unsigned coff[NCOPY], soff[NCOPY];  // element offset within the tile's cell (channel) / smem byte offset
+#pragma unroll
+    for (int k = 0; k < NCOPY; ++k) {
+        const int q = tid + k * DW_THREADS;
+        if (q < NXCH) {
+            const int cc = q % XC, col = (q / XC) % (DW_TILE + 2), r = q / (XC * (DW_TILE + 2));
+            crow[k] = r;
+            ccol[k] = col;
+            coff[k] = (unsigned)(cc * 8);
+            soff[k] = (unsigned)((r * (DW_TILE + 2) + col) * L::XSTR + cc * 16);
+        } else if (q < NXCH + NGCH) {
+            const int qq = q - NXCH, cc = qq % GC, cell = qq / GC;
+            crow[k] = -1;
+            ccol[k] = cell;
+            coff[k] = (unsigned)(cc * 8);
+            soff[k] = (unsigned)(L::RAW_X + cell * L::GSTR + cc * 16);
+        } else {
+            crow[k] = -2;
+            ccol[k] = 0;
+            coff[k] = 0;
+            soff[k] = 0;
+        }
+    }
     auto stage = [&](int t, int b) {
         const int img = t / tiles_img, rem = t % tiles_img, y = rem / tiles_x, x0 = (rem % tiles_x) * DW_TILE;
-        unsigned char* rx = sm + b * L::RAW;
-        unsigned char* rg = rx + L::RAW_X;
-        constexpr int XC = CIN / 8, GC = COUT / 8;
-        for (int i = tid; i < 3 * (DW_TILE + 2) * XC; i += DW_THREADS) {
-            const int cc = i % XC, col = (i / XC) % (DW_TILE + 2), r = i / (XC * (DW_TILE + 2));
-            const int gy = y + r - 1, gx = x0 + col - 1;
-            const bool in = gy >= 0 && gy < H && gx >= 0 && gx < W;
-            const __nv_bfloat16* src = in ? x + ((((size_t)img * H + gy) * W + gx) * CIN + cc * 8) : x;
-            cp_async16(reinterpret_cast<unsigned*>(rx + (r * (DW_TILE + 2) + col) * L::XSTR + cc * 16), src, in);
-        }
-        for (int i = tid; i < DW_TILE * GC; i += DW_THREADS) {
-            const int cc = i % GC, cell = i / GC;
-            cp_async16(reinterpret_cast<unsigned*>(rg + cell * L::GSTR + cc * 16),
-                       g + ((((size_t)img * H + y) * W + x0 + cell) * COUT + cc * 8), true);
+        unsigned char* raw = sm + b * L::RAW;
+        const size_t rowx = ((size_t)img * H + y) * W;  // cell index of (img, y, 0)
+#pragma unroll
+        for (int k = 0; k < NCOPY; ++k) {
+            if (crow[k] >= 0) {
+                const int gy = y + crow[k] - 1, gx = x0 + ccol[k] - 1;
+                const bool in = gy >= 0 && gy < H && gx >= 0 && gx < W;
+                const __nv_bfloat16* src =
+                    in ? x + (size_t)((long long)rowx + (long long)(crow[k] - 1) * W + gx) * CIN + coff[k] : x;
+                cp_async16(reinterpret_cast<unsigned*>(raw + soff[k]), src, in);
+            } else if (crow[k] == -1) {
+                cp_async16(reinterpret_cast<unsigned*>(raw + soff[k]), g + (rowx + x0 + ccol[k]) * COUT + coff[k], true);
+            }
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    // operands of raw buffer b into operand buffer b: A (9 CIN rows) and B (COUT rows), K = 64
-    auto transpose = [&](int b) {
-        const unsigned rx = su32(sm + b * L::RAW), rg = rx + L::RAW_X;
-        unsigned char* A = sm + L::OFF_A + b * L::A_BYTES;
-        unsigned char* Bm = sm + L::OFF_B + b * L::B_BYTES;
-        constexpr int JA = 9 * (CIN / 8) * 8, JB = (COUT / 8) * 8;  // core matrices (multiples of 4)
-        for (int u = warp; u < (JA + JB) / 4; u += DW_THREADS / 32) {
-            const int job = 4 * u + (lane >> 3), j = lane & 7;  // this thread's row address
-            unsigned addr;
-            if (job < JA) {
-                const int kc = job % 8, cg = (job / 8) % (CIN / 8), tap = job / (8 * (CIN / 8));
-                const int dy = tap / 3, dx = tap % 3;  // raw row dy holds image row y + dy - 1
-                addr = rx + (unsigned)((dy * (DW_TILE + 2) + kc * 8 + j + dx) * L::XSTR + cg * 16);
-            } else {
-                const int q = job - JA, kc = q % 8, ng = q / 8;
-                addr = rg + (unsigned)((kc * 8 + j) * L::GSTR + ng * 16);
-            }
+    // operands of a raw buffer into an operand buffer: A (9 CIN rows) and B (COUT rows), K = 64.
+    // One ldmatrix.x4.trans covers 4 consecutive k chunks of one 8-row group: for A, op (tap, cg,
+    // kh) reads the input rows' cells kh*32 + 8 (lane / 8) + lane % 8 shifted by the tap; for B, op
+    // (ng, kh) the gradient cells.  The lane's part is a constant; the rest is warp-uniform.
+    constexpr int OPA = 9 * XC * 2, OPB = GC * 2;
+    const unsigned lane_src_x = (unsigned)(((lane >> 3) * 8 + (lane & 7)) * L::XSTR);
+    const unsigned lane_src_g = (unsigned)(((lane >> 3) * 8 + (lane & 7)) * L::GSTR);
+    auto transpose = [&](int rb, int b) {
+        const unsigned rx = su32(sm + rb * L::RAW);
+        unsigned char* A = sm + L::OFF_A + b * L::A_BYTES + 4 * lane;
+        unsigned char* Bm = sm + L::OFF_B + b * L::B_BYTES + 4 * lane;
+        for (int op = warp; op < OPA + OPB; op += DW_THREADS / 32) {
             unsigned r[4];
-            ldsm_x4_trans(r, addr);
-#pragma unroll
-            for (int q4 = 0; q4 < 4; ++q4) {
-                const int jb = 4 * u + q4;
-                unsigned char* dst;
-                if (jb < JA) {
-                    const int kc = jb % 8, cg = (jb / 8) % (CIN / 8), tap = jb / (8 * (CIN / 8));
-                    dst = A + (kc * L::MTOT + tap * CIN + cg * 8) * 16;
-                } else {
-                    const int q = jb - JA, kc = q % 8, ng = q / 8;
-                    dst = Bm + (kc * COUT + ng * 8) * 16;
-                }
-                *reinterpret_cast<unsigned*>(dst + 4 * lane) = r[q4];
+            unsigned char* dst;
+            unsigned stride;
+            if (op < OPA) {
+                const int kh = op & 1, cg = (op >> 1) % XC, tap = (op >> 1) / XC;
+                const int dy = tap / 3, dx = tap % 3;  // raw row dy holds image row y + dy - 1
+                ldsm_x4_trans(r, rx + lane_src_x + (unsigned)((dy * (DW_TILE + 2) + kh * 32 + dx) * L::XSTR + cg * 16));
+                dst = A + ((kh * 4) * L::MTOT + tap * CIN + cg * 8) * 16;
+                stride = L::MTOT * 16;
+            } else {
+                const int q = op - OPA, kh = q & 1, ng = q >> 1;
+                ldsm_x4_trans(r, rx + L::RAW_X + lane_src_g + (unsigned)((kh * 32) * L::GSTR + ng * 16));
+                dst = Bm + ((kh * 4) * COUT + ng * 8) * 16;
+                stride = COUT * 16;
             }
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) *reinterpret_cast<unsigned*>(dst + q4 * stride) = r[q4];
         }
     };
 
@@ -566,18 +593,25 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
     constexpr uint32_t ID = idesc_bf16(128, COUT);
     bool alive = true;
     int i = 0, last = -1;
+    // the copies of the first two tiles (an empty group when there is no second tile, so that
+    // one group per tile is always outstanding)
+    const int G = (int)gridDim.x;
     if ((int)blockIdx.x < ntiles) stage(blockIdx.x, 0);
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+    if ((int)blockIdx.x + G < ntiles) stage(blockIdx.x + G, 1);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+    for (int t = blockIdx.x; t < ntiles; t += G, ++i) {
         const int b = i & 1;
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // tile i's copies (tile i + 1's may run)
         if (tid == 0) s_ok = i < 2 || bar_wait_bounded(bar0 + 8 * b, ((i - 2) >> 1) & 1) ? 1 : 0;
         __syncthreads();
         if (!s_ok) {
             alive = false;
             break;
         }
-        transpose(b);
-        if (t + (int)gridDim.x < ntiles) stage(t + (int)gridDim.x, b ^ 1);
+        transpose(i % L::NRAW, b);
+        // raw buffer (i + 2) % 3 was last read by the transposes of tile i - 1
+        if (t + 2 * G < ntiles) stage(t + 2 * G, (i + 2) % L::NRAW);
+        else asm volatile("cp.async.commit_group;" ::: "memory");
         fence_async_smem();
         fence_before();
         __syncthreads();
