@@ -426,46 +426,56 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 // Weight gradients of one layer on the tensor cores (training):
 //   dW[tap][ci][co] = sum_cells x[cell + off(tap)][ci] g[cell][co],   db[co] = sum_cells g[cell][co]
 // over every cell of nimg images of H x W (W % 64 == 0; inputs outside an image read as zero),
-// as one GEMM per CTA with the cells as the K dimension: A = the 9 shifted input windows stacked
-// along M (row tap * CIN + ci, plus a row of ones whose product is db, zero rows up to a multiple
-// of 128), B = the output gradients (N = COUT), D in tensor memory, accumulated over all the
-// CTA's tiles.  A tile is 64 cells of one image row (K = 64: 4 MMAs of K16 per M tile).
+// as GEMMs with the cells as the K dimension: for each row tap dy, A = the three column-shifted
+// copies of the input row y + dy - 1 stacked along M (row dx * CIN + ci, a row of ones whose
+// product is db, zero rows up to 128), B = the output gradients of row y (N = COUT), D in
+// tensor memory (columns dy * COUT), accumulated over all the CTA's tiles.  A tile is 64 cells
+// of one image row (K = 64: 4 MMAs of K16 per row tap).
 //
-// Staging.  The tile's 3 input rows (66 cells each, x0 - 1 .. x0 + 64) and its 64 gradient cells
-// are copied as they are stored (NHWC, channels contiguous) into shared memory with cp.async;
-// ldmatrix.trans then turns each 8-cell x 8-channel block into the canonical K-major core matrix
-// (8 rows = channels, 16 bytes = 8 cells): thread t of the warp receives exactly the 4 bytes at
-// offset 4t of the core matrix, so the stores are contiguous.  Operand layout [k chunk][row][8]:
-// the descriptor's leading (K) offset is rows * 16, its stride (8-row) offset 128, as in the
-// inference kernel.  Raw tiles go through a ring of three buffers (the copies of the next two
-// tiles are in flight while a tile is transposed) and the operands are double-buffered: the
-// transposes of tile i overlap the MMAs of tile i - 1; before operand buffer b is rewritten,
-// thread 0 waits (1 s limit) for the commit of the MMAs that read it.  The address arithmetic
-// that does not depend on the tile is done once.  Each CTA writes its partial sums in the
-// CUDA-core kernel's layout, so k_dweight_final reduces them the same way.
+// Sliding rows.  The tiles are numbered down the rows of each 64-column strip of each image, and
+// a CTA takes a contiguous range of them, so consecutive tiles are consecutive rows of a strip:
+// the transposed copies of an input row live in one of four slots (row r in slot (r + 1) % 4)
+// and serve the three tiles that read it.  A tile transposes one new input row (the row below),
+// or three where its strip starts, while the MMAs of the previous tile may still read theirs.
+// (A ring one tile deeper -- five slots, three gradient buffers -- measured no faster: the
+// per-tile work on the SM, not the wait for the MMAs, sets the pace.)
+//
+// Staging.  The input rows and the tile's 64 gradient cells are copied as they are stored (NHWC,
+// channels contiguous) into shared memory with cp.async, through a ring of three raw buffers (the
+// copies of the next two tiles are in flight while a tile is transposed); ldmatrix.trans turns
+// each 8-cell x 8-channel block into the canonical K-major core matrix (8 rows = channels, 16
+// bytes = 8 cells): thread t of the warp receives exactly the 4 bytes at offset 4t of the core
+// matrix, so the stores are contiguous.  Operand layout [k chunk][row][8]: the descriptor's
+// leading (K) offset is rows * 16, its stride (8-row) offset 128, as in the inference kernel.
+// Gradients are double-buffered.  Before a slot or gradient buffer is rewritten, thread 0 waits
+// (1 s limit) for the commit of the MMAs that read it: the tile two back, or the previous tile
+// where a strip starts.  Each CTA
+// writes its partial sums in the CUDA-core kernel's layout, so k_dweight_final reduces them the
+// same way.
 constexpr int DW_TILE = 64;
 constexpr int DW_THREADS = 256;
 constexpr int DW_TMEM_COLS = 128;
 
 template <int CIN, int COUT>
 struct DwLayout {
-    static constexpr int MROWS = 9 * CIN + 1;  // shifted inputs and the ones row
-    static constexpr int MT = (MROWS + 127) / 128;
-    static constexpr int MTOT = MT * 128;
-    static constexpr int XSTR = CIN * 2 + 16;  // padded: ldmatrix rows 8 cells apart hit distinct banks
+    static constexpr int SROWS = 128;               // rows of a slot: 3 CIN shifted rows, ones, zeros
+    static constexpr int SLOT = 8 * SROWS * 16;     // [k chunk 8][128 rows][16 B]
+    static constexpr int NSLOT = 4;                 // input-row slots: 3 read + 1 being filled
+    static constexpr int NB = 2;                    // gradient buffers (and mbarriers)
+    static constexpr int XSTR = CIN * 2 + 16;       // padded: ldmatrix rows 8 cells apart hit distinct banks
     static constexpr int GSTR = COUT * 2 + 16;
     static constexpr int RAW_X = 3 * (DW_TILE + 2) * XSTR;
     static constexpr int RAW = ((RAW_X + DW_TILE * GSTR + 127) / 128) * 128;
-    static constexpr int A_BYTES = MTOT * DW_TILE * 2;
+    static constexpr int NRAW = 3;                  // raw ring depth
     static constexpr int B_BYTES = COUT * DW_TILE * 2;
-    static constexpr int NRAW = 3;  // raw ring depth
-    static constexpr int OFF_A = NRAW * RAW;
-    static constexpr int OFF_B = OFF_A + 2 * A_BYTES;
-    static constexpr int OFF_BAR = OFF_B + 2 * B_BYTES;
-    static constexpr int OFF_TSLOT = OFF_BAR + 16;
+    static constexpr int OFF_SLOT = NRAW * RAW;
+    static constexpr int OFF_B = OFF_SLOT + NSLOT * SLOT;
+    static constexpr int OFF_BAR = OFF_B + NB * B_BYTES;
+    static constexpr int OFF_TSLOT = OFF_BAR + 8 * NB;
     static constexpr int SMEM = OFF_TSLOT + 16;
-    static_assert(MT * COUT <= DW_TMEM_COLS, "accumulators fit the allocation");
-    static_assert(OFF_A % 128 == 0 && OFF_B % 128 == 0 && OFF_BAR % 8 == 0, "alignment");
+    static_assert(3 * CIN + 1 <= SROWS, "three shifted rows and the ones row fit a slot");
+    static_assert(3 * COUT <= DW_TMEM_COLS, "accumulators fit the allocation");
+    static_assert(OFF_SLOT % 128 == 0 && OFF_B % 128 == 0 && OFF_BAR % 8 == 0, "alignment");
     static_assert(SMEM <= 227 * 1024, "one CTA per SM");
 };
 
@@ -483,20 +493,22 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const unsigned bar0 = su32(sm + L::OFF_BAR);  // one mbarrier per operand buffer, 8 bytes apart
+    const unsigned bar0 = su32(sm + L::OFF_BAR);  // one mbarrier per gradient buffer, 8 bytes apart
     unsigned* tslot = reinterpret_cast<unsigned*>(sm + L::OFF_TSLOT);
-    const int tiles_x = W / DW_TILE, tiles_img = H * tiles_x, ntiles = nimg * tiles_img;
+    const int tiles_x = W / DW_TILE, ntiles = nimg * tiles_x * H;
+    // this CTA's tiles: a contiguous range of t = (img * tiles_x + strip) * H + y
+    const int G = (int)gridDim.x;
+    const int t_begin = (int)(((long long)ntiles * blockIdx.x) / G), t_end = (int)(((long long)ntiles * (blockIdx.x + 1)) / G);
 
-    // rows of A that no tile writes: the ones row (db) and the zero rows, in both buffers
-    for (int i = tid; i < 2 * 8 * (L::MTOT - 9 * CIN); i += DW_THREADS) {
-        const int b = i / (8 * (L::MTOT - 9 * CIN)), rem = i % (8 * (L::MTOT - 9 * CIN));
-        const int kc = rem / (L::MTOT - 9 * CIN), m = 9 * CIN + rem % (L::MTOT - 9 * CIN);
-        const unsigned v = m == 9 * CIN ? 0x3F803F80u : 0u;  // BF16 1.0 pairs
-        *reinterpret_cast<uint4*>(sm + L::OFF_A + b * L::A_BYTES + (kc * L::MTOT + m) * 16) = make_uint4(v, v, v, v);
+    // rows of the slots that no tile writes: the ones row (db) and the zero rows
+    for (int i = tid; i < L::NSLOT * 8 * (L::SROWS - 3 * CIN); i += DW_THREADS) {
+        const int per = 8 * (L::SROWS - 3 * CIN);
+        const int sl = i / per, rem = i % per, kc = rem / (L::SROWS - 3 * CIN), m = 3 * CIN + rem % (L::SROWS - 3 * CIN);
+        const unsigned v = m == 3 * CIN ? 0x3F803F80u : 0u;  // BF16 1.0 pairs
+        *reinterpret_cast<uint4*>(sm + L::OFF_SLOT + sl * L::SLOT + (kc * L::SROWS + m) * 16) = make_uint4(v, v, v, v);
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        for (int k = 0; k < L::NB; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8 * k) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -506,13 +518,15 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
 
-    // raw copies of tile t into raw buffer b: 3 input rows of 66 cells and 64 gradient cells.
-    // Thread tid copies the 16-byte chunks tid, tid + 256, ... of the tile, the same in every tile.
+    // raw copies of tile t into raw buffer b: the input rows it needs first (rows y - 1 .. y + 1
+    // into raw rows 0 .. 2 where its strip starts in this CTA, else row y + 1 into raw row 2) and
+    // its 64 gradient cells.  Thread tid copies the 16-byte chunks tid, tid + 256, ... of the
+    // buffer, the same in every tile.
     constexpr int XC = CIN / 8, GC = COUT / 8;
     constexpr int NXCH = 3 * (DW_TILE + 2) * XC, NGCH = DW_TILE * GC;
     constexpr int NCOPY = (NXCH + NGCH + DW_THREADS - 1) / DW_THREADS;
     int crow[NCOPY], ccol[NCOPY];  // input chunk: raw row, column (-1: a gradient chunk; -2: none)
-    unsigned coff[NCOPY], soff[NCOPY];  // element offset within the tile's cell (channel) / smem byte offset
+    unsigned coff[NCOPY], soff[NCOPY];  // channel offset within the cell / smem byte offset
 #pragma unroll
     for (int k = 0; k < NCOPY; ++k) {
         const int q = tid + k * DW_THREADS;
@@ -535,13 +549,15 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
             soff[k] = 0;
         }
     }
+    auto starts = [&](int t) { return t == t_begin || t % H == 0; };  // a strip starts: three new rows
     auto stage = [&](int t, int b) {
-        const int img = t / tiles_img, rem = t % tiles_img, y = rem / tiles_x, x0 = (rem % tiles_x) * DW_TILE;
+        const int y = t % H, strip = t / H, img = strip / tiles_x, x0 = (strip % tiles_x) * DW_TILE;
+        const int first = starts(t) ? 0 : 2;
         unsigned char* raw = sm + b * L::RAW;
         const size_t rowx = ((size_t)img * H + y) * W;  // cell index of (img, y, 0)
 #pragma unroll
         for (int k = 0; k < NCOPY; ++k) {
-            if (crow[k] >= 0) {
+            if (crow[k] >= first) {
                 const int gy = y + crow[k] - 1, gx = x0 + ccol[k] - 1;
                 const bool in = gy >= 0 && gy < H && gx >= 0 && gx < W;
                 const __nv_bfloat16* src =
@@ -553,29 +569,33 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    // operands of a raw buffer into an operand buffer: A (9 CIN rows) and B (COUT rows), K = 64.
-    // One ldmatrix.x4.trans covers 4 consecutive k chunks of one 8-row group: for A, op (tap, cg,
-    // kh) reads the input rows' cells kh*32 + 8 (lane / 8) + lane % 8 shifted by the tap; for B, op
-    // (ng, kh) the gradient cells.  The lane's part is a constant; the rest is warp-uniform.
-    constexpr int OPA = 9 * XC * 2, OPB = GC * 2;
+    // operands of tile t from raw buffer rb: each new input row r (raw row r - y + 1) into slot
+    // (r + 1) % 4 as three column-shifted copies (slot row dx * CIN + ci holds the cells shifted
+    // by dx - 1), and the gradients into gradient buffer gb.  One ldmatrix.x4.trans covers 4
+    // consecutive k chunks of one 8-row group; the lane's part of the source address is a
+    // constant, the rest is warp-uniform.
+    constexpr int OPR = 3 * XC * 2, OPB = GC * 2;  // ops per input row, per gradient row
     const unsigned lane_src_x = (unsigned)(((lane >> 3) * 8 + (lane & 7)) * L::XSTR);
     const unsigned lane_src_g = (unsigned)(((lane >> 3) * 8 + (lane & 7)) * L::GSTR);
-    auto transpose = [&](int rb, int b) {
+    auto transpose = [&](int t, int rb, int gb) {
+        const int y = t % H;
+        const int first = starts(t) ? 0 : 2, nops = (3 - first) * OPR + OPB;
         const unsigned rx = su32(sm + rb * L::RAW);
-        unsigned char* A = sm + L::OFF_A + b * L::A_BYTES + 4 * lane;
-        unsigned char* Bm = sm + L::OFF_B + b * L::B_BYTES + 4 * lane;
-        for (int op = warp; op < OPA + OPB; op += DW_THREADS / 32) {
+        unsigned char* S = sm + L::OFF_SLOT + 4 * lane;
+        unsigned char* Bm = sm + L::OFF_B + gb * L::B_BYTES + 4 * lane;
+        for (int op = warp; op < nops; op += DW_THREADS / 32) {
             unsigned r[4];
             unsigned char* dst;
             unsigned stride;
-            if (op < OPA) {
-                const int kh = op & 1, cg = (op >> 1) % XC, tap = (op >> 1) / XC;
-                const int dy = tap / 3, dx = tap % 3;  // raw row dy holds image row y + dy - 1
-                ldsm_x4_trans(r, rx + lane_src_x + (unsigned)((dy * (DW_TILE + 2) + kh * 32 + dx) * L::XSTR + cg * 16));
-                dst = A + ((kh * 4) * L::MTOT + tap * CIN + cg * 8) * 16;
-                stride = L::MTOT * 16;
+            if (op < (3 - first) * OPR) {
+                const int rr = first + op / OPR, o = op % OPR;  // raw row, op within the row
+                const int kh = o & 1, cg = (o >> 1) % XC, dx = (o >> 1) / XC;
+                ldsm_x4_trans(r, rx + lane_src_x + (unsigned)((rr * (DW_TILE + 2) + kh * 32 + dx) * L::XSTR + cg * 16));
+                const int slot = (y + rr) % L::NSLOT;  // input row y + rr - 1
+                dst = S + slot * L::SLOT + ((kh * 4) * L::SROWS + dx * CIN + cg * 8) * 16;
+                stride = L::SROWS * 16;
             } else {
-                const int q = op - OPA, kh = q & 1, ng = q >> 1;
+                const int q = op - (3 - first) * OPR, kh = q & 1, ng = q >> 1;
                 ldsm_x4_trans(r, rx + L::RAW_X + lane_src_g + (unsigned)((kh * 32) * L::GSTR + ng * 16));
                 dst = Bm + ((kh * 4) * COUT + ng * 8) * 16;
                 stride = COUT * 16;
@@ -591,70 +611,86 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
     fence_after();
     const unsigned tmem = *tslot;
     constexpr uint32_t ID = idesc_bf16(128, COUT);
+    // operand descriptors of slot 0 and gradient buffer 0 at k chunk 0 (shared memory is below
+    // 256 KB, so adding an offset / 16 to the start address field never carries out of it)
+    const uint64_t a_desc0 = sdesc(su32(sm + L::OFF_SLOT), L::SROWS * 16, 128);
+    const uint64_t b_desc0 = sdesc(su32(sm + L::OFF_B), COUT * 16, 128);
     bool alive = true;
     int i = 0, last = -1;
     // the copies of the first two tiles (an empty group when there is no second tile, so that
     // one group per tile is always outstanding)
-    const int G = (int)gridDim.x;
-    if ((int)blockIdx.x < ntiles) stage(blockIdx.x, 0);
-    if ((int)blockIdx.x + G < ntiles) stage(blockIdx.x + G, 1);
+    if (t_begin < t_end) stage(t_begin, 0);
+    if (t_begin + 1 < t_end) stage(t_begin + 1, 1);
     else asm volatile("cp.async.commit_group;" ::: "memory");
-    for (int t = blockIdx.x; t < ntiles; t += G, ++i) {
-        const int b = i & 1;
+    for (int t = t_begin; t < t_end; ++t, ++i) {
+        const int b = i % L::NB;
         asm volatile("cp.async.wait_group 1;" ::: "memory");  // tile i's copies (tile i + 1's may run)
-        if (tid == 0) s_ok = i < 2 || bar_wait_bounded(bar0 + 8 * b, ((i - 2) >> 1) & 1) ? 1 : 0;
+        if (tid == 0) {
+            // the slot this tile fills and gradient buffer b were last read by tile i - NB; where a
+            // strip starts, three slots are refilled: wait for the previous tile (and so all)
+            bool ok = i < L::NB || bar_wait_bounded(bar0 + 8 * b, ((i - L::NB) / L::NB) & 1);
+            if (ok && starts(t) && i >= 1) ok = bar_wait_bounded(bar0 + 8 * ((i - 1) % L::NB), ((i - 1) / L::NB) & 1);
+            s_ok = ok ? 1 : 0;
+        }
         __syncthreads();
         if (!s_ok) {
             alive = false;
             break;
         }
-        transpose(i % L::NRAW, b);
+        transpose(t, i % L::NRAW, b);
         // raw buffer (i + 2) % 3 was last read by the transposes of tile i - 1
-        if (t + 2 * G < ntiles) stage(t + 2 * G, (i + 2) % L::NRAW);
+        if (t + 2 < t_end) stage(t + 2, (i + 2) % L::NRAW);
         else asm volatile("cp.async.commit_group;" ::: "memory");
         fence_async_smem();
         fence_before();
         __syncthreads();
         if (tid == 0) {
             fence_after();
-            const unsigned a0 = su32(sm + L::OFF_A + b * L::A_BYTES), b0 = su32(sm + L::OFF_B + b * L::B_BYTES);
+            const int y = t % H;
+            // descriptors differ only in their start address field (address / 16, low bits)
 #pragma unroll
-            for (int mt = 0; mt < L::MT; ++mt)
+            for (int dy = 0; dy < 3; ++dy) {
+                const uint64_t ad0 = a_desc0 + (uint64_t)((((y + dy) % L::NSLOT) * L::SLOT) >> 4);  // input row y + dy - 1
 #pragma unroll
-                for (int ks = 0; ks < DW_TILE / 16; ++ks) {
-                    const uint64_t ad = sdesc(a0 + (unsigned)((2 * ks * L::MTOT + mt * 128) * 16), L::MTOT * 16, 128);
-                    const uint64_t bd = sdesc(b0 + (unsigned)(2 * ks * COUT * 16), COUT * 16, 128);
-                    mma(tmem + (unsigned)(mt * COUT), ad, bd, ID, (i > 0 || ks > 0) ? 1u : 0u);
-                }
+                for (int ks = 0; ks < DW_TILE / 16; ++ks)
+                    mma(tmem + (unsigned)(dy * COUT), ad0 + (uint64_t)((2 * ks * L::SROWS * 16) >> 4),
+                        b_desc0 + (uint64_t)((b * L::B_BYTES + 2 * ks * COUT * 16) >> 4), ID, (i > 0 || ks > 0) ? 1u : 0u);
+            }
             commit(bar0 + 8 * b);
         }
         last = i;
     }
     // the last commit covers every MMA of the CTA
-    if (tid == 0) s_ok = (last < 0 || bar_wait_bounded(bar0 + 8 * (last & 1), (last >> 1) & 1)) ? 1 : 0;
+    if (tid == 0) s_ok = (last < 0 || bar_wait_bounded(bar0 + 8 * (last % L::NB), (last / L::NB) & 1)) ? 1 : 0;
     __syncthreads();
     if (!s_ok) alive = false;
     if (alive && last >= 0) {
         fence_after();
+        // accumulator rows: row tap dy's tile, row dx * CIN + ci = tap (3 dy + dx), channel ci;
+        // row 3 CIN of every tile is db (read from dy = 1)
         const int lane_q = warp & 3, half = warp >> 2;
         float* p = partials + (size_t)blockIdx.x * (9 * CIN * COUT + COUT);
-        for (int mt = half; mt < L::MT; mt += 2) {
-            const int m = mt * 128 + lane_q * 32 + lane;
+        for (int dy = half; dy < 3; dy += 2) {
+            const int m = lane_q * 32 + lane;
 #pragma unroll
             for (int c0 = 0; c0 < COUT; c0 += 16) {
                 float v[16];
-                tmem_ld16(tmem + ((unsigned)(lane_q * 32) << 16) + (unsigned)(mt * COUT + c0), v);
-                float* o = m < 9 * CIN ? p + (size_t)m * COUT + c0 : (m == 9 * CIN ? p + 9 * CIN * COUT + c0 : nullptr);
+                tmem_ld16(tmem + ((unsigned)(lane_q * 32) << 16) + (unsigned)(dy * COUT + c0), v);
+                float* o = m < 3 * CIN ? p + (size_t)(dy * 3 * CIN + m) * COUT + c0
+                                       : (m == 3 * CIN && dy == 1 ? p + 9 * CIN * COUT + c0 : nullptr);
                 if (o != nullptr)
 #pragma unroll
                     for (int j = 0; j < 16; ++j) o[j] = v[j];
             }
         }
+    } else if (last < 0) {  // no tile: zero partials
+        float* p = partials + (size_t)blockIdx.x * (9 * CIN * COUT + COUT);
+        for (int k = tid; k < 9 * CIN * COUT + COUT; k += DW_THREADS) p[k] = 0.0f;
     }
     if (!alive) {  // a wait ran out: record it and let the MMAs in flight finish before freeing
         if (tid == 0) {
             atomicExch(status, LBM_ERR_TIMEOUT);
-            if (last >= 0) bar_wait_bounded(bar0 + 8 * (last & 1), (last >> 1) & 1);
+            if (last >= 0) bar_wait_bounded(bar0 + 8 * (last % L::NB), (last / L::NB) & 1);
         }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
