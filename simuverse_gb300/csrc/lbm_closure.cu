@@ -585,9 +585,31 @@ int pack(lbm_closure* c) {
     return LBM_OK;
 }
 
+// one 3x3 convolution of nimg images: the training path's (zero padding) on the tcgen05 tensor
+// cores with the FUSED kernels, else on the mma.sync layer kernel
 template <int CIN, int COUT, int EPI, bool PER>
 int conv(lbm_closure* c, const __nv_bfloat16* in, void* out, const __nv_bfloat16* w, const float* bias,
          const __nv_bfloat16* mask, int nimg, int H, int W) {
+    if (!PER && c->kernel == LBM_CLOSURE_KERNEL_FUSED) {
+        using L = cl::tc::ConvTcLayout<CIN, COUT>;
+        static lbm::PerDevice<bool> attr_tc;  // the attribute is set per device (c's device is current)
+        bool done_tc = false;
+        C_CK(attr_tc.get(
+            c->device,
+            [](bool& v) {
+                v = true;
+                return cudaFuncSetAttribute(cl::tc::k_conv_tc<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            L::SMEM);
+            },
+            &done_tc));
+        const dim3 grid((unsigned)((W + 127) / 128), (unsigned)((H + cl::tc::CONV_TC_ROWS - 1) / cl::tc::CONV_TC_ROWS),
+                        (unsigned)nimg);
+        cl::tc::k_conv_tc<CIN, COUT, EPI><<<grid, cl::tc::CONV_TC_THREADS, L::SMEM, c->stream>>>(in, out, w, bias, mask, H,
+                                                                                              W, c->d_status);
+        C_CK(cudaGetLastError());
+        ++c->launches;
+        return LBM_OK;
+    }
     constexpr size_t smem = cl::conv_smem_bytes<CIN, COUT>();
     static lbm::PerDevice<bool> attr;  // the attribute is set per device (c's device is current)
     bool done = false;

@@ -703,4 +703,195 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// One 3x3 convolution of the training path on the tcgen05 tensor cores, the same operation as
+// k_conv3x3 (non-periodic: cells outside an image read as zero): in [nimg][H][W][CIN] BF16,
+// wk [9][COUT][CIN] BF16 (tap = 3 (dy + 1) + (dx + 1)), bias [COUT] FP32; out [nimg][H][W][COUT]
+// BF16 with bias and ReLU (EPI_BIAS_RELU), FP32 with bias (EPI_BIAS_F32), or BF16 where the mask
+// activation is positive (EPI_MASK, the input gradient of a ReLU layer).
+//
+// The inference kernel's schedule for one layer: a CTA owns 128 output columns (positions
+// x0 .. x0 + 127 = MMA rows) and CONV_TC_ROWS output rows and walks its input rows y0 - 1 ..
+// y0 + CONV_TC_ROWS.  Each input row (130 positions, x0 - 1 .. x0 + 128) is read once: per column
+// shift dx and 16-channel chunk one MMA multiplies the 128 positions starting at dx by the three
+// row taps' weights side by side (N = 3 COUT), the row-tap blocks stored in the order [2, 1, 0, 2,
+// 1] so that output row o always lands in accumulator slot o mod 3.  After input row r the output
+// row r - 1 is complete: its slot is read, the epilogue written to global memory and the slot
+// zeroed.  Input rows are double-buffered and copied with cp.async while the MMAs of the row
+// before run; thread 0 waits (1 s limit) for each row's commit, and a wait that runs out records
+// LBM_ERR_TIMEOUT, waits (bounded) for the MMAs in flight and frees the tensor memory.
+constexpr int CONV_TC_ROWS = 16;
+constexpr int CONV_TC_THREADS = 256;
+constexpr int CONV_TC_TMEM = 128;
+
+template <int CIN, int COUT>
+struct ConvTcLayout {
+    static constexpr int GIN = CIN / 8;                       // 8-channel groups of an input row
+    static constexpr int IN_ROW = GIN * PLANE;                // [group][130 positions][16 B]
+    static constexpr int OFF_W = 2 * IN_ROW;                  // [dx 3][group][block 5][cout][16 B]
+    static constexpr int W_BYTES = 3 * GIN * 5 * COUT * 16;
+    static constexpr int OFF_BIAS = OFF_W + W_BYTES;
+    static constexpr int OFF_BAR = OFF_BIAS + COUT * 4;
+    static constexpr int OFF_TSLOT = OFF_BAR + 8;
+    static constexpr int SMEM = ((OFF_TSLOT + 4 + 127) / 128) * 128;
+    static_assert(CIN % 16 == 0 && (COUT == 16 || COUT == 32), "channel counts of the closure layers");
+    static_assert(3 * COUT <= CONV_TC_TMEM, "accumulator slots fit the allocation");
+    static_assert(OFF_W % 16 == 0 && OFF_BAR % 8 == 0, "alignment");
+};
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(CONV_TC_THREADS, 2)
+    k_conv_tc(const __nv_bfloat16* __restrict__ in, void* __restrict__ out, const __nv_bfloat16* __restrict__ wk,
+              const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, int H, int W,
+              int* __restrict__ status) {
+    using L = ConvTcLayout<CIN, COUT>;
+    constexpr int KC = CIN / 16;
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int img = blockIdx.z, y0 = blockIdx.y * CONV_TC_ROWS, x0 = blockIdx.x * 128;
+    const size_t img_off = (size_t)img * H * W;
+    unsigned char* ring = sm;
+    float* sbias = reinterpret_cast<float*>(sm + L::OFF_BIAS);
+    const unsigned bar = su32(sm + L::OFF_BAR);
+    unsigned* tslot = reinterpret_cast<unsigned*>(sm + L::OFF_TSLOT);
+
+    // weights to the operand layout, row-tap block i holding tap dy = (2 - i) mod 3
+    for (int i = tid; i < 3 * L::GIN * 5 * COUT; i += CONV_TC_THREADS) {  // (dx, group, block, cout)
+        const int n = i % COUT, blk = (i / COUT) % 5, g = (i / (5 * COUT)) % L::GIN, dx = i / (5 * COUT * L::GIN);
+        const int t = 3 * ((2 - blk + 3) % 3) + dx;
+        *reinterpret_cast<uint4*>(sm + L::OFF_W + i * 16) =
+            *reinterpret_cast<const uint4*>(wk + ((size_t)t * COUT + n) * CIN + g * 8);
+    }
+    if (EPI != EPI_MASK && tid < COUT) sbias[tid] = bias[tid];
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)),
+                     "r"(CONV_TC_TMEM)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // input row gy (zero outside the image) into ring buffer b: group g, position p = column x0 - 1 + p
+    auto stage = [&](int gy, int b) {
+        unsigned char* row = ring + b * L::IN_ROW;
+        for (int i = tid; i < L::GIN * POS; i += CONV_TC_THREADS) {
+            const int p = i % POS, g = i / POS, gx = x0 - 1 + p;
+            const bool ok = gy >= 0 && gy < H && gx >= 0 && gx < W;
+            const __nv_bfloat16* src = ok ? in + (img_off + (size_t)gy * W + gx) * CIN + g * 8 : in;
+            cp_async16(reinterpret_cast<unsigned*>(row + g * PLANE + p * 16), src, ok);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    stage(y0 - 1, 0);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tmem = *tslot;
+    const int lane_q = warp & 3, half = warp >> 2;
+    const unsigned lane_off = (unsigned)(lane_q * 32) << 16;
+    constexpr int HC = COUT / 2;  // accumulator columns per warpgroup
+    // every slot starts at zero (each warpgroup its half of the columns)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if constexpr (HC == 16) tmem_zero16(tmem + lane_off + k * COUT + half * HC);
+        else tmem_zero8(tmem + lane_off + k * COUT + half * HC);
+    }
+    tmem_wait_st();
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    unsigned parity = 0u;
+    bool alive = true;
+    const int nrows = min(CONV_TC_ROWS, H - y0);  // output rows of this CTA
+    for (int a = 0; a < nrows + 2; ++a) {  // input row y0 - 1 + a
+        const int gy = y0 - 1 + a;
+        if (tid == 0) {
+            fence_after();
+            issue_row<KC, COUT>(tmem, su32(ring + (a & 1) * L::IN_ROW), gy, su32(sm + L::OFF_W));
+            commit(bar);
+        }
+        if (a + 1 < nrows + 2) stage(gy + 1, (a + 1) & 1);  // its buffer was read by row a - 1's MMAs
+        if (tid == 0) s_ok = bar_wait_bounded(bar, parity) ? 1 : 0;
+        __syncthreads();
+        if (!s_ok) {
+            alive = false;
+            break;
+        }
+        bar_try(bar, parity);  // complete: acquire the phase in every thread
+        parity ^= 1u;
+        fence_after();
+        // output row gy - 1 is complete; rows before y0 only had to be cleared
+        const int go = gy - 1;
+        const int slot = ((go % 3) + 3) % 3;
+        const unsigned t = tmem + lane_off + slot * COUT + half * HC;
+        const int p = lane_q * 32 + lane, gx = x0 + p;
+        if (go >= y0) {
+            float v[HC];
+            if constexpr (HC == 16) tmem_ld16(t, v);
+            else tmem_ld8(t, v);
+            if (gx < W) {
+                const size_t cell = img_off + (size_t)go * W + gx;
+                const int c0 = half * HC;
+                if (EPI == EPI_BIAS_F32) {
+                    float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + cell * COUT + c0);
+#pragma unroll
+                    for (int q = 0; q < HC / 4; ++q)
+                        o[q] = make_float4(v[4 * q] + sbias[c0 + 4 * q], v[4 * q + 1] + sbias[c0 + 4 * q + 1],
+                                           v[4 * q + 2] + sbias[c0 + 4 * q + 2], v[4 * q + 3] + sbias[c0 + 4 * q + 3]);
+                } else {
+                    unsigned w[HC / 2];
+                    if (EPI == EPI_BIAS_RELU) {
+#pragma unroll
+                        for (int q = 0; q < HC / 2; ++q)
+                            w[q] = pack_bf16x2(fmaxf(v[2 * q] + sbias[c0 + 2 * q], 0.0f),
+                                               fmaxf(v[2 * q + 1] + sbias[c0 + 2 * q + 1], 0.0f));
+                    } else {  // EPI_MASK
+                        const uint4* mk = reinterpret_cast<const uint4*>(mask + cell * COUT + c0);
+#pragma unroll
+                        for (int q4 = 0; q4 < HC / 8; ++q4) {
+                            const uint4 mm = mk[q4];
+                            const unsigned mw[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) {
+                                const __nv_bfloat162 m2 = *reinterpret_cast<const __nv_bfloat162*>(&mw[q]);
+                                const int k = 8 * q4 + 2 * q;
+                                w[4 * q4 + q] = pack_bf16x2(__bfloat162float(m2.x) > 0.0f ? v[k] : 0.0f,
+                                                            __bfloat162float(m2.y) > 0.0f ? v[k + 1] : 0.0f);
+                            }
+                        }
+                    }
+                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) + cell * COUT + c0);
+#pragma unroll
+                    for (int q = 0; q < HC / 8; ++q) o[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+                }
+            }
+        }
+        if constexpr (HC == 16) tmem_zero16(t);
+        else tmem_zero8(t);
+        tmem_wait_st();
+        asm volatile("cp.async.wait_group 0;" ::: "memory");  // input row a + 1 landed
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+    }
+    if (!alive) {  // a wait ran out: record it and let the MMAs in flight finish before freeing
+        if (tid == 0) {
+            atomicExch(status, LBM_ERR_TIMEOUT);
+            bar_wait_bounded(bar, parity);
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(CONV_TC_TMEM)
+                     : "memory");
+    }
+}
+
 }  // namespace tc

@@ -130,10 +130,11 @@ def test_gradients_match_fp64_restatement(gpu, projection, crop):
 
 @pytest.mark.parametrize("target", ["populations", "stress"])
 @pytest.mark.parametrize("crop", [64, 128])
-def test_tensor_core_weight_gradients_match_cuda_core_ones(gpu, target, crop):
-    """The training step's weight and bias gradients from the tcgen05 kernel (crops a multiple of
-    64 wide) equal the CUDA-core kernel's up to FP32 summation order, for every layer: both sum
-    the same BF16 products."""
+def test_tensor_core_training_matches_layer_kernels(gpu, target, crop):
+    """The training step on the tcgen05 kernels (convolutions and weight gradients, FUSED) against
+    the mma.sync convolutions and CUDA-core weight gradients (LAYERS): both round the same FP32
+    sums of BF16 products to BF16 activations, so the losses and every layer's gradient agree up
+    to the rare activation whose rounding the summation order flips."""
     rng = np.random.default_rng(7)
     c = Closure(128, 128, seed=3, inputs="eq", target=target, projection="cell")
     c.params = _random_params(c, rng)
@@ -145,7 +146,7 @@ def test_tensor_core_weight_gradients_match_cuda_core_ones(gpu, target, crop):
     c.set_kernel("fused")
     loss_b, g_b = c.loss_grad(feats, targets)
     c.status()
-    assert loss_a == loss_b  # same forward kernels for training
+    assert abs(loss_a - loss_b) <= 1e-4 * abs(loss_a), (loss_a, loss_b)
     off, prev = 0, 0.0
     for n in (9 * 9 * 32, 32, 9 * 32 * 32, 32, 9 * 32 * 9, 9):
         a, b = g_a[off:off + n].astype(np.float64), g_b[off:off + n].astype(np.float64)
@@ -153,7 +154,7 @@ def test_tensor_core_weight_gradients_match_cuda_core_ones(gpu, target, crop):
         # a bias block is measured against its layer's weight block too: the stress loss does not
         # depend on the last bias, whose gradient is rounding noise
         scale = max(np.linalg.norm(a), prev if n in (32, 9) else 0.0)
-        assert np.linalg.norm(a - b) <= 1e-5 * scale, (n, np.linalg.norm(a - b), scale)
+        assert np.linalg.norm(a - b) <= 2e-3 * scale, (n, np.linalg.norm(a - b), scale)
         prev = np.linalg.norm(a)
     c.close()
 
