@@ -720,7 +720,7 @@ __global__ void __launch_bounds__(DW_THREADS, 1)
 // zeroed.  Input rows are double-buffered and copied with cp.async while the MMAs of the row
 // before run; thread 0 waits (1 s limit) for each row's commit, and a wait that runs out records
 // LBM_ERR_TIMEOUT, waits (bounded) for the MMAs in flight and frees the tensor memory.
-constexpr int CONV_TC_ROWS = 16;
+constexpr int CONV_TC_ROWS = 8;
 constexpr int CONV_TC_THREADS = 256;
 constexpr int CONV_TC_TMEM = 128;
 
@@ -740,7 +740,7 @@ struct ConvTcLayout {
 };
 
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(CONV_TC_THREADS, 2)
+__global__ void __launch_bounds__(CONV_TC_THREADS, 4)
     k_conv_tc(const __nv_bfloat16* __restrict__ in, void* __restrict__ out, const __nv_bfloat16* __restrict__ wk,
               const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask, int H, int W,
               int* __restrict__ status) {
