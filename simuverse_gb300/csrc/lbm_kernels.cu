@@ -195,10 +195,11 @@ __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __re
     for (int i = 0; i < 9; ++i) {
         const R eu = R(EX(i)) * ux + R(EY(i)) * uy;
         const R d = PW<R>(i) * (drho + rho * (R(3) * eu + R(4.5) * (eu * eu) - usq));
-        const size_t k = pop_index(tiled, N, i, c);
-        ST::st(A + k, d);
-        ST::st(B + k, d);
+        ST::st(A + pop_index(tiled, N, i, c), d);
     }
+    // B's fluid cells are left as they are: every step writes all of them before anything reads
+    // B (a step reads only the current buffer), and its solid cells, which no step writes, are
+    // cleared above
     macro[c] = (float)rho; macro[c + N] = (float)ux; macro[c + 2 * N] = (float)uy;
 }
 
