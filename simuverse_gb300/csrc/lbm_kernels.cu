@@ -214,13 +214,13 @@ __global__ void k_phys_init(typename ST::T* __restrict__ A, typename ST::T* __re
 // rho w (1 - 1.5 u.u + 4.5 (e.u)^2), and the odd part 3 rho w (e.u), and multiply-adds left
 // to the compiler: about half the instructions, so the step runs at memory speed.
 // ------------------------------------------------------------------------------------
-// resident blocks of TPB threads per SM the fast reference-mode step is compiled for (16: 32
-// registers, full occupancy)
-#ifndef LBM_REF_FAST_MIN_BLOCKS
-#define LBM_REF_FAST_MIN_BLOCKS 16
+// resident blocks of TPB threads per SM the reference-mode step is compiled for (16: 32
+// registers, full occupancy; both arithmetic forms fit without spills with 32-bit indices)
+#ifndef LBM_REF_MIN_BLOCKS
+#define LBM_REF_MIN_BLOCKS 16
 #endif
 template <bool MACRO, class IDX, bool FAST>
-__global__ void __launch_bounds__(TPB, FAST ? LBM_REF_FAST_MIN_BLOCKS : 0) k_ref_step(const float* __restrict__ A, float* __restrict__ B,
+__global__ void __launch_bounds__(TPB, LBM_REF_MIN_BLOCKS) k_ref_step(const float* __restrict__ A, float* __restrict__ B,
                                                   uint16_t* __restrict__ flags, lbm_lattice_info* __restrict__ info,
                                                   float omega, int nx, int ny, float* __restrict__ macro) {
     const int x = blockIdx.x * TPB + threadIdx.x;
