@@ -795,20 +795,20 @@ def main():
                     help="--workload reference: arithmetic of the reference-rule step")
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snapshots", type=int, default=125)
-    ap.add_argument("--interval", type=int, default=256)
+    ap.add_argument("--interval", type=int, default=512)
     ap.add_argument("--dagger", type=int, default=0)
     ap.add_argument("--inputs", default="eq", choices=["eq", "neq"])
     ap.add_argument("--target", default="stress", choices=["momentum", "equilibrium", "populations", "stress"])
-    ap.add_argument("--window", type=int, default=64, help="coarse steps per training pair (0: --k-coarse)")
+    ap.add_argument("--window", type=int, default=128, help="coarse steps per training pair (0: --k-coarse)")
     ap.add_argument("--crop", type=int, default=256, help="training crop side (coarse cells)")
     ap.add_argument("--projection", default="cell", choices=["domain", "cell"])
     ap.add_argument("--sources", nargs="+", default=["fresh"], choices=["fresh", "rollout"])
     ap.add_argument("--k-coarse", type=int, default=4)
-    ap.add_argument("--train-iters", type=int, default=3000)
+    ap.add_argument("--train-iters", type=int, default=8000)
     ap.add_argument("--train-blocks", type=int, default=10)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-seeds", type=int, nargs="*", default=[9001, 9002])
-    ap.add_argument("--strengths", type=float, nargs="*", default=[1.0, 0.5, 0.25, 0.1],
+    ap.add_argument("--strengths", type=float, nargs="*", default=[1.0, 0.5, 0.35, 0.25],
                     help="closure correction strengths tried on the validation seed")
     ap.add_argument("--val-seed", type=int, default=7001)
     ap.add_argument("--check-every", type=int, default=2000)
