@@ -786,7 +786,7 @@ def main():
     ap.add_argument("--extras-size", type=int, default=8192)
     ap.add_argument("--min-seconds", type=float, default=2.0,
                     help="repeat the K-step interval until about this much device time is timed")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2", "tiled"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "vec4", "bulk", "vec2", "tiled", "ring"])
     ap.add_argument("--rounding", default="nearest", choices=["nearest", "stochastic"],
                     help="rounding of 16-bit population stores")
     ap.add_argument("--workload", default="channel",

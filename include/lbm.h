@@ -86,6 +86,10 @@ extern "C" {
                                (the nine planes of 64 cells stored together; FP16 / BF16, BGK,
                                nx % 64 == 0); read-back and checkpoints are layout-independent
                                except that a checkpoint loads only into the same layout */
+#define LBM_KERNEL_RING 6   /* the tiled layout and rules of LBM_KERNEL_TILED (same results bit
+                               for bit), its rows staged in shared memory by bulk asynchronous
+                               copies: blocks walk down strips of 8 tiles with a ring of rows
+                               (slower than LBM_KERNEL_TILED on GB300) */
 
 /* physics-mode collision */
 #define LBM_COLLISION_BGK 0          /* single relaxation time */

@@ -28,7 +28,7 @@ LBM_ERR_NOMEM = -7
 MODES = {"reference": 0, "physics": 1}
 DTYPES = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
 SCENES = {"poiseuille": 0, "cavity": 1, "custom": 2, "channel": 3, "periodic": 4}
-KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3, "vec2": 4, "tiled": 5}
+KERNELS = {"auto": 0, "cell": 1, "vec4": 2, "bulk": 3, "vec2": 4, "tiled": 5, "ring": 6}
 COLLISIONS = {"bgk": 0, "regularized": 1, "mrt": 2, "kbc": 3}
 ROUNDINGS = {"nearest": 0, "stochastic": 1}
 ARITHS = {"exact": 0, "fast": 1}

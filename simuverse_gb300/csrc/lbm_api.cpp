@@ -354,9 +354,9 @@ int validate_params(const lbm_params& p) {
         return fail(LBM_ERR_ARG, "scene %d exists in physics mode only", p.scene);
     if (!(p.tau > 0.0f) || !std::isfinite(p.tau)) return fail(LBM_ERR_ARG, "tau must be positive and finite");
     if (p.pixel_size < 1) return fail(LBM_ERR_ARG, "pixel_size must be >= 1");
-    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_TILED) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
-    if (p.kernel == LBM_KERNEL_TILED && !lbm::tiled_layout_eligible(p))
-        return fail(LBM_ERR_ARG, "the tiled kernel needs physics mode, FP16 or BF16 storage, BGK and nx %% 64 == 0");
+    if (p.kernel < LBM_KERNEL_AUTO || p.kernel > LBM_KERNEL_RING) return fail(LBM_ERR_ARG, "unknown kernel %d", p.kernel);
+    if ((p.kernel == LBM_KERNEL_TILED || p.kernel == LBM_KERNEL_RING) && !lbm::tiled_layout_eligible(p))
+        return fail(LBM_ERR_ARG, "the tiled kernels need physics mode, FP16 or BF16 storage, BGK and nx %% 64 == 0");
     if (p.collision < LBM_COLLISION_BGK || p.collision > LBM_COLLISION_KBC)
         return fail(LBM_ERR_ARG, "unknown collision %d", p.collision);
     if (p.collision != LBM_COLLISION_BGK && p.mode != LBM_MODE_PHYSICS)
@@ -367,8 +367,8 @@ int validate_params(const lbm_params& p) {
     if (p.rounding == LBM_ROUNDING_STOCHASTIC) {
         if (p.mode != LBM_MODE_PHYSICS || (p.dtype != LBM_DTYPE_F16 && p.dtype != LBM_DTYPE_BF16))
             return fail(LBM_ERR_ARG, "stochastic rounding applies to physics-mode FP16 / BF16 storage");
-        if (p.kernel != LBM_KERNEL_AUTO && p.kernel != LBM_KERNEL_TILED && p.kernel != LBM_KERNEL_VEC2 &&
-            p.kernel != LBM_KERNEL_CELL)
+        if (p.kernel != LBM_KERNEL_AUTO && p.kernel != LBM_KERNEL_TILED && p.kernel != LBM_KERNEL_RING &&
+            p.kernel != LBM_KERNEL_VEC2 && p.kernel != LBM_KERNEL_CELL)
             return fail(LBM_ERR_ARG, "stochastic rounding runs on the tiled, two-cell and one-cell kernels");
     }
     if (p.kernel == LBM_KERNEL_VEC2 && (p.mode != LBM_MODE_PHYSICS || p.nx % 2 != 0))
@@ -568,7 +568,8 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
     h->ny = p.ny;
     h->N = (size_t)p.nx * p.ny;
     h->fluid_ty = (p.scene == LBM_SCENE_CAVITY) ? 1 : 0;
-    h->tiled = (p.kernel == LBM_KERNEL_TILED || p.kernel == LBM_KERNEL_AUTO) && lbm::tiled_layout_eligible(p);
+    h->tiled = (p.kernel == LBM_KERNEL_TILED || p.kernel == LBM_KERNEL_RING || p.kernel == LBM_KERNEL_AUTO) &&
+               lbm::tiled_layout_eligible(p);
     h->tau = p.tau;
     h->omega = 1.0f / p.tau;
     h->omega_d = 1.0 / (double)p.tau;

@@ -137,6 +137,7 @@ bool vec_step_supported(const lbm_handle* h);
 cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s);
 cudaError_t launch_phys_step_vec2(lbm_handle* h, bool write_macro, cudaStream_t s);
 cudaError_t launch_phys_step_tiled(lbm_handle* h, bool write_macro, cudaStream_t s);
+cudaError_t launch_phys_step_ring(lbm_handle* h, bool write_macro, cudaStream_t s);
 // the tiled layout applies: physics mode, 16-bit storage, BGK, nx % POP_TILE == 0, 9 N < 2^32
 bool tiled_layout_eligible(const lbm_params& p);
 // bulk-copy fed physics step (lbm_step_bulk.cu)

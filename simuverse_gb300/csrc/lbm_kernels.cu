@@ -731,7 +731,9 @@ cudaError_t launch_step(lbm_handle* h, bool write_macro, cudaStream_t s) {
             default: return write_macro ? phys_step_t<StoreBF16, true>(h, s) : phys_step_t<StoreBF16, false>(h, s);
         }
     }
-    if (h->tiled) return launch_phys_step_tiled(h, write_macro, s);
+    if (h->tiled)
+        return h->p.kernel == LBM_KERNEL_RING ? launch_phys_step_ring(h, write_macro, s)
+                                              : launch_phys_step_tiled(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_BULK) return launch_phys_step_bulk(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC4) return launch_phys_step_vec(h, write_macro, s);
     if (h->p.kernel == LBM_KERNEL_VEC2) return launch_phys_step_vec2(h, write_macro, s);

@@ -83,3 +83,81 @@ def test_tiled_rejected_where_it_does_not_apply(gpu):
         FluidSimulator(100, 64, mode="physics", dtype="f16", scene="cavity", kernel="tiled")  # nx % 64
     with pytest.raises(Exception):
         FluidSimulator(128, 64, mode="physics", dtype="f32", scene="cavity", kernel="tiled")  # FP32
+
+
+# LBM_KERNEL_RING: the tiled kernel's rules with the rows staged in shared memory by bulk copies.
+# Strips of 8 tiles, so 576 = 9 tiles leaves a one-tile strip, 64 is a lattice of one tile, and
+# 4 or 5 rows wrap inside one block's row range.
+RING_CASES = [("channel", 576, 37), ("channel", 1024, 300), ("cavity", 128, 64), ("periodic", 512, 4),
+              ("periodic", 64, 5), ("periodic", 192, 7)]
+
+
+def _bits(sim):
+    return sim.read_populations().view(np.uint32)
+
+
+@pytest.mark.parametrize("rounding", ["nearest", "stochastic"])
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+@pytest.mark.parametrize("scene,nx,ny", RING_CASES)
+def test_ring_matches_tiled_bit_for_bit(gpu, scene, nx, ny, dtype, rounding):
+    kw = dict(mode="physics", dtype=dtype, scene=scene, tau=0.58, lid_speed=0.1, inlet_speed=0.05, seed=5,
+              disk_radius=(4.0, 9.0), rounding=rounding)
+    a = FluidSimulator(nx, ny, kernel="ring", **kw)
+    b = FluidSimulator(nx, ny, kernel="tiled", **kw)
+    if scene == "periodic":
+        rng = np.random.default_rng(3)
+        u = (0.02 * rng.standard_normal((2, ny, nx))).astype(np.float32)
+        a.init_equilibrium(None, u[0], u[1])
+        b.init_equilibrium(None, u[0], u[1])
+    a.step(37)
+    b.step(37)
+    if scene == "channel":  # a force stroke and an obstacle: forcing cells and new walls mid-run
+        for s in (a, b):
+            s.add_external_force((nx * 0.4, ny * 0.5), (nx * 0.35, ny * 0.45))
+            if ny >= 64:  # the obstacle is a disc of radius 28
+                s.add_obstacle(nx // 2, ny // 2)
+    a.step(40)
+    b.step(40)
+    a.status()
+    assert np.array_equal(_bits(a), _bits(b))
+    for x, y in zip(a.read_macro(), b.read_macro()):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+def test_ring_macro_every_step_and_full_size(gpu, dtype):
+    """The macro-writing form, and the 4096^2 channel (one wave of blocks, 8 strips)."""
+    for nx, ny, steps in ((640, 200, 25), (4096, 4096, 6)):
+        kw = dict(mode="physics", dtype=dtype, scene="channel", tau=0.56, inlet_speed=0.05, seed=11,
+                  macro_every_step=True)
+        a = FluidSimulator(nx, ny, kernel="ring", **kw)
+        b = FluidSimulator(nx, ny, kernel="tiled", **kw)
+        a.step(steps)
+        b.step(steps)
+        a.status()
+        assert np.array_equal(_bits(a), _bits(b))
+        for x, y in zip(a.read_macro(), b.read_macro()):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+        a.close()
+        b.close()
+
+
+def test_ring_checkpoint_shares_the_tiled_layout(gpu, tmp_path):
+    kw = dict(mode="physics", dtype="f16", scene="cavity", tau=0.6, lid_speed=0.1)
+    a = FluidSimulator(128, 64, kernel="ring", **kw)
+    a.step(10)
+    path = str(tmp_path / "r.ckpt")
+    a.save(path)
+    b = FluidSimulator(128, 64, kernel="tiled", **kw)
+    b.load(path)
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(_bits(a), _bits(b))
+    a.close()
+    b.close()
+    with pytest.raises(Exception):
+        FluidSimulator(100, 64, mode="physics", dtype="f16", scene="cavity", kernel="ring")  # nx % 64
+    with pytest.raises(Exception):
+        FluidSimulator(128, 64, mode="physics", dtype="f32", scene="cavity", kernel="ring")  # FP32
