@@ -289,7 +289,7 @@ int lbm_load(lbm_handle* h, const char* path);
    lbm_conservation (bit-identical for the same populations), computed over device
    buffers the caller owns: d_populations in the storage format of (mode, dtype) -- 9
    planes of nx*ny values, absolute f for reference mode, f - w (FP16: times 2^10) for
-   physics mode; the tiled 16-bit layout of LBM_KERNEL_TILED is not accepted (its sums would
+   physics mode; the tiled 16-bit layout of LBM_KERNEL_TILED / _RING is not accepted (its sums would
    be wrong without an error), so take such state from a handle with the SoA layout --
    d_info (device, nx*ny records; needed in physics mode to skip solids),
    d_out (device, 3 doubles).  For callers that cannot allocate device memory: a host
@@ -334,7 +334,7 @@ int lbm_kernel_launches(const lbm_handle* h, uint64_t* launches);
 int lbm_device_macro(lbm_handle* h, float** rho, float** ux, float** uy);
 /* the population buffer the next step reads, in the handle's storage format (see
    lbm_conservation_noalloc), valid until the next lbm_step, reset, load or destroy; *tiled
-   (may be NULL) = 1 when it is in the tiled 16-bit layout of LBM_KERNEL_TILED, 0 for the
+   (may be NULL) = 1 when it is in the tiled 16-bit layout of LBM_KERNEL_TILED / _RING, 0 for the
    plane-major SoA layout.  No counterpart in the reference. */
 int lbm_device_populations(lbm_handle* h, void** d_state, int32_t* tiled);
 
