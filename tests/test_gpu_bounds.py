@@ -6,7 +6,8 @@ inside the buffers.
 
 The child process loads the checked build (SIMUVERSE_LBM_VARIANT=bounds) and runs each kernel
 family -- the reference-mode step (exact and fast), the one-cell physics step (FP32, FP64,
-FP16), the tiled 16-bit step, the bulk-copy step and the batched form -- over odd lattice sizes
+FP16), the tiled 16-bit step (global loads and rows staged in shared memory), the bulk-copy
+step and the batched form -- over odd lattice sizes
 (4x4, 5x7, 300x5, 1032x66 and the nearest sizes each kernel accepts) with obstacles on the
 cells next to the walls and in the corners, inlet, outlet and forcing cells, for a few steps
 with the macro field written every step; the record must stay empty.  The self-test first
@@ -113,6 +114,19 @@ def child_main():
                 s.sync()
                 s.close()
                 check("tiled %s %dx%d %s" % (dtype, nx, ny, scene))
+                runs += 1
+    # the same layout stepped from rows staged in shared memory (strips of 8 tiles: 576 = 9 tiles)
+    for nx, ny in ((64, 4), (576, 5), (1024, 66)):
+        for scene in ("cavity", "channel"):
+            for dtype, rnd in (("f16", "stochastic"), ("bf16", "nearest")):
+                s = FluidSimulator(nx, ny, mode="physics", scene=scene, dtype=dtype, kernel="ring", rounding=rnd,
+                                   tau=0.6, lid_speed=0.05, inlet_speed=0.03, disk_radius=(1.0, 2.0),
+                                   macro_every_step=True)
+                s.set_info(_forcing_cells(_wall_obstacles(s.info(), nx), ny))
+                s.step(6)
+                s.status()
+                s.close()
+                check("ring %s %dx%d %s" % (dtype, nx, ny, scene))
                 runs += 1
     # bulk-copy kernel (nx % 8 == 0)
     for nx, ny in ((8, 4), (296, 7), (1032, 66), (520, 5)):
