@@ -158,9 +158,9 @@ cudaError_t launch_phys_step_vec(lbm_handle* h, bool write_macro, cudaStream_t s
 // before reusing the slot.  No block barrier in the loop: warps drift apart by up to
 // RING_SLOTS - 3 rows, and the bytes in flight are set by the ring depth, not by registers.
 //
-// Measured on GB300 at 8192^2 FP16 it runs below the tiled kernel (129 against 158 GLUPS): a
-// strip moves at the pace of its slowest warp (a tile next to a solid takes the general
-// per-cell rules), and the ring's shared memory allows 4 blocks (32 consumer warps) per SM.  It
+// Measured on GB300 at 8192^2 FP16 it runs below the tiled kernel on the 5 %-solid channel
+// (129 against 158 GLUPS): a strip moves at the pace of its slowest warp, and a tile next to a
+// solid takes the general per-cell rules.  Without solids the two run alike (161 and 162).  It
 // is kept as LBM_KERNEL_RING; LBM_KERNEL_AUTO takes the tiled kernel.
 //
 // Every wait is bounded (1 s).  A consumer warp that gives up records LBM_ERR_TIMEOUT in the
