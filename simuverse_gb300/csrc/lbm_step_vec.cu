@@ -188,7 +188,7 @@ struct RingLayout {
     static constexpr int MIN_BLOCKS = NSLOT <= 5 ? 4 : (NSLOT <= 7 ? 3 : 2);
 };
 
-// the halo piece of direction j among the three with the same e_x (1, 5, 8 and 3, 6, 7)
+// the halo pair of direction j among the three with the same e_x (1, 5, 8 and 3, 6, 7)
 __host__ __device__ constexpr int halo_rank(int j) { return (j == 1 || j == 3) ? 0 : ((j == 5 || j == 6) ? 1 : 2); }
 
 __device__ __forceinline__ unsigned ring_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
