@@ -255,3 +255,39 @@ def test_no_gpu_fails_loudly():
         BatchSimulator(generate_domains(4, 1))
     with pytest.raises(nat.LbmError):
         Closure(64, 64)
+
+
+def test_python_tables_match_the_header():
+    """The Python mirror's name tables and status codes are the header's #define values."""
+    import re
+
+    from simuverse_gb300 import _native as nat
+
+    text = open(os.path.join(ROOT, "include", "lbm.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define (LBM_[A-Z0-9_]+) +\(?(-?\d+)\)?", text)}
+    for prefix, table in (("LBM_MODE_", nat.MODES), ("LBM_DTYPE_", nat.DTYPES), ("LBM_SCENE_", nat.SCENES),
+                          ("LBM_KERNEL_", nat.KERNELS), ("LBM_COLLISION_", nat.COLLISIONS),
+                          ("LBM_ROUNDING_", nat.ROUNDINGS), ("LBM_ARITH_", nat.ARITHS)):
+        header = {k[len(prefix):].lower(): v for k, v in defs.items() if k.startswith(prefix)}
+        assert header == table, prefix
+    for name in ("ARG", "CUDA", "TIMEOUT", "NAN", "IO", "STATE", "NOMEM"):
+        assert defs["LBM_ERR_" + name] == getattr(nat, "LBM_ERR_" + name)
+
+
+@pytest.mark.parametrize("dtype,nx,kernel", [
+    (0, 128, 6),   # the ring-staged tiled step on FP32
+    (2, 100, 6),   # nx % 64
+    (2, 100, 5),   # the tiled step, nx % 64
+    (2, 128, 7),   # unknown kernel
+])
+def test_create_rejects_kernels_where_they_do_not_apply(native, dtype, nx, kernel):
+    from simuverse_gb300 import _native as nat
+
+    p = nat.LbmParams()
+    native.lbm_params_default(ctypes.byref(p))
+    p.nx, p.ny, p.mode, p.dtype, p.kernel = nx, 64, 1, dtype, kernel
+    p.scene = nat.SCENES["periodic"]
+    h = ctypes.c_void_p()
+    assert native.lbm_create(ctypes.byref(p), ctypes.byref(h)) == nat.LBM_ERR_ARG
+    assert h.value is None
+    assert "kernel" in native.lbm_last_error().decode()
