@@ -398,25 +398,32 @@ void ensure_host_info(lbm_handle* h) {
 
 // the physics-mode scene mask built on the device: the host samples the channel's disk list
 // only (a few thousand numbers) and uploads that instead of the records
-int build_scene_on_device(lbm_handle* h) {
-    std::vector<double> disks;
+// Physics-mode scenes built on the device, with the initial state.  The base pattern (walls,
+// inlet, outlet, lid) and the initialisation are launched first, so the GPU runs them while the
+// host draws the channel's disk list; rasterising the disks then marks their cells solid and
+// gives them the state the initialisation gives a solid cell (disk cells are bulk cells of the
+// base pattern), which is the state of initialising the finished scene.  The disk list stays
+// in the handle until the caller's sync: its copy to the device reads it.
+int init_state(lbm_handle* h);
+
+int scene_and_state_on_device(lbm_handle* h) {
+    LBM_CK(lbm::launch_build_scene(h, h->stream));
+    ++h->launches;
+    LBM_TRY(init_state(h));
+    h->scene_disks.clear();
     if (h->p.scene == LBM_SCENE_CHANNEL)
-        disks = channel_disks(h->nx, h->ny, h->p.seed, h->p.solid_fraction, h->p.disk_rmin, h->p.disk_rmax);
-    double* d_disks = nullptr;
-    const int nd = (int)(disks.size() / 3);
+        h->scene_disks = channel_disks(h->nx, h->ny, h->p.seed, h->p.solid_fraction, h->p.disk_rmin, h->p.disk_rmax);
+    const int nd = (int)(h->scene_disks.size() / 3);
     if (nd > 0) {
-        LBM_CK(pool_alloc(&d_disks, disks.size() * sizeof(double), h->stream));
-        cudaError_t e = cudaMemcpyAsync(d_disks, disks.data(), disks.size() * sizeof(double), cudaMemcpyHostToDevice,
-                                        h->stream);
-        if (e == cudaSuccess) e = lbm::launch_build_scene(h, d_disks, nd, h->stream);
-        pool_free(d_disks, h->stream);  // ordered after the kernels that read it
-        // the host list is read by the copy: it must not go away before the copy ran
-        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        double* d_disks = nullptr;
+        LBM_CK(pool_alloc(&d_disks, h->scene_disks.size() * sizeof(double), h->stream));
+        cudaError_t e = cudaMemcpyAsync(d_disks, h->scene_disks.data(), h->scene_disks.size() * sizeof(double),
+                                        cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) e = lbm::launch_raster_disks(h, d_disks, nd, true, h->stream);
+        pool_free(d_disks, h->stream);  // ordered after the kernel that reads it
         if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "scene mask on the device: %s", cudaGetErrorString(e));
-    } else {
-        LBM_CK(lbm::launch_build_scene(h, nullptr, 0, h->stream));
+        ++h->launches;
     }
-    h->launches += nd > 0 ? 2 : 1;
     h->host_info.clear();
     h->host_info_lazy = true;
     return LBM_OK;
@@ -594,14 +601,16 @@ int lbm_create(const lbm_params* pin, lbm_handle** out) {
     }
     int r = LBM_OK;
     if (device_scene(p)) {
-        r = build_scene_on_device(h);
+        r = scene_and_state_on_device(h);  // also initialises the state
     } else {
         build_scene_mask(p, h->host_info);
         r = upload_info_rows(h, 0, h->ny);
+        if (r == LBM_OK) r = init_state(h);
     }
     if (r == LBM_OK) r = rebuild_flags(h);
-    if (r == LBM_OK) r = init_state(h);
-    if (r == LBM_OK) r = sync(h);
+    const int rs = sync(h);                  // also after a failed launch: the copy reads the list
+    h->scene_disks = std::vector<double>();
+    if (r == LBM_OK) r = rs;
     if (r != LBM_OK) {
         free_all(h);
         delete h;
@@ -666,18 +675,23 @@ int lbm_reset(lbm_handle* h) {
     LBM_TRY(check_handle(h));
     LBM_TRY(use_device(h));
     // reference: only the Poiseuille scene rebuilds its mask (d2q9_node.rs:248-255)
+    int r = LBM_OK;
     if (device_scene(h->p)) {
-        LBM_TRY(build_scene_on_device(h));  // the host copy follows lazily, as after create
-        h->host_mirror_valid = false;       // the device copy of the host copy is stale
-    } else if (h->p.mode == LBM_MODE_PHYSICS || h->p.scene == LBM_SCENE_POISEUILLE) {
-        build_scene_mask(h->p, h->host_info);
-        h->host_info_lazy = false;
-        LBM_TRY(upload_info_rows(h, 0, h->ny));
+        r = scene_and_state_on_device(h);  // the host copy follows lazily, as after create
+        h->host_mirror_valid = false;      // the device copy of the host copy is stale
+    } else {
+        if (h->p.mode == LBM_MODE_PHYSICS || h->p.scene == LBM_SCENE_POISEUILLE) {
+            build_scene_mask(h->p, h->host_info);
+            h->host_info_lazy = false;
+            r = upload_info_rows(h, 0, h->ny);
+        }
+        if (r == LBM_OK) r = init_state(h);
     }
-    LBM_TRY(rebuild_flags(h));
-    LBM_TRY(init_state(h));
+    if (r == LBM_OK) r = rebuild_flags(h);
     h->pre_x = h->pre_y = 0.0f;  // fluid_simulator.rs:214
-    return sync(h);
+    const int rs = sync(h);      // also before the disk list is released on a failed launch
+    h->scene_disks = std::vector<double>();
+    return r != LBM_OK ? r : rs;
 }
 
 int lbm_set_tau(lbm_handle* h, float tau) {

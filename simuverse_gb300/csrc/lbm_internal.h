@@ -41,6 +41,7 @@ struct lbm_handle {
     uint16_t* d_flags = nullptr;
     lbm_lattice_info* d_info = nullptr;
     std::vector<lbm_lattice_info> host_info;  // D2Q9Node::lattice_info_data
+    std::vector<double> scene_disks;  // the channel's disk list while its upload may still read it
     bool host_info_lazy = false;  // host_info not built yet: the scene mask was built on the device
     float* d_macro = nullptr;                 // rho, ux, uy planes
     double* d_part = nullptr;                 // reduction partials
@@ -127,7 +128,10 @@ inline size_t dtype_size(int dtype) { return dtype == LBM_DTYPE_F64 ? 8 : (dtype
 cudaError_t launch_build_flags(const lbm_handle* h, cudaStream_t s);
 // physics-mode scene mask on the device: base pattern of p's scene, then the disks
 // (cx, cy, r triples in device memory) as obstacles
-cudaError_t launch_build_scene(lbm_handle* h, const double* d_disks, int ndisks, cudaStream_t s);
+cudaError_t launch_build_scene(lbm_handle* h, cudaStream_t s);  // walls, inlet, outlet, lid
+// the channel's disks into the info records; clear_state: also the solid-cell state in the
+// populations and macro planes of an initialised lattice
+cudaError_t launch_raster_disks(lbm_handle* h, const double* d_disks, int ndisks, bool clear_state, cudaStream_t s);
 cudaError_t launch_ref_init(lbm_handle* h, cudaStream_t s);
 cudaError_t launch_phys_init(lbm_handle* h, const float* d_rho, const float* d_ux, const float* d_uy,
                              cudaStream_t s);

@@ -104,24 +104,54 @@ __global__ void k_build_scene(lbm_lattice_info* __restrict__ info, int nx, int n
 
 // one block per disk: the lattice points of its bounding box inside [1, nx-2] x [1, ny-2]
 // with (x - cx)^2 + (y - cy)^2 <= r^2 become obstacles
-__global__ void k_raster_disks(lbm_lattice_info* __restrict__ info, int nx, int ny, const double* __restrict__ disks) {
+// A disk's cells become obstacles.  With A non-null the lattice was initialised before the
+// disks were drawn (lbm_create, lbm_reset): each disk cell also gets the state the
+// initialisation gives a solid cell -- zero populations in both buffers (all-zero bits in every
+// storage format, at pop_index of the handle's layout) and a zero macro value.
+__global__ void k_raster_disks(lbm_lattice_info* __restrict__ info, int nx, int ny, const double* __restrict__ disks,
+                               unsigned char* __restrict__ A, unsigned char* __restrict__ B, int elem_bytes,
+                               bool tiled, float* __restrict__ macro) {
     const double cx = disks[3 * blockIdx.x], cy = disks[3 * blockIdx.x + 1], r = disks[3 * blockIdx.x + 2];
     const int x0 = (int)floor(__dsub_rn(cx, r)), x1 = (int)ceil(__dadd_rn(cx, r));
     const int y0 = (int)floor(__dsub_rn(cy, r)), y1 = (int)ceil(__dadd_rn(cy, r));
     const int w = x1 - x0 + 1, n = w * (y1 - y0 + 1);
     const double r2 = __dmul_rn(r, r);
+    const size_t N = (size_t)nx * ny;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int x = x0 + i % w, y = y0 + i / w;
         if (x < 1 || x > nx - 2 || y < 1 || y > ny - 2) continue;
         const double dx = __dsub_rn((double)x, cx), dy = __dsub_rn((double)y, cy);
-        if (__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) <= r2) info[(size_t)y * nx + x].material = LBM_OBSTACLE;
+        if (__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) > r2) continue;
+        const size_t c = (size_t)y * nx + x;
+        info[c].material = LBM_OBSTACLE;
+        if (A) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const size_t b = pop_index(tiled, N, j, c) * (size_t)elem_bytes;
+                if (elem_bytes == 2) {
+                    *reinterpret_cast<uint16_t*>(A + b) = 0; *reinterpret_cast<uint16_t*>(B + b) = 0;
+                } else if (elem_bytes == 4) {
+                    *reinterpret_cast<uint32_t*>(A + b) = 0u; *reinterpret_cast<uint32_t*>(B + b) = 0u;
+                } else {
+                    *reinterpret_cast<uint64_t*>(A + b) = 0ull; *reinterpret_cast<uint64_t*>(B + b) = 0ull;
+                }
+            }
+            macro[c] = 0.0f; macro[c + N] = 0.0f; macro[c + 2 * N] = 0.0f;
+        }
     }
 }
 
-cudaError_t launch_build_scene(lbm_handle* h, const double* d_disks, int ndisks, cudaStream_t s) {
+cudaError_t launch_build_scene(lbm_handle* h, cudaStream_t s) {
     const dim3 grid((unsigned)((h->nx + 255) / 256), (unsigned)h->ny);
     k_build_scene<<<grid, 256, 0, s>>>(h->d_info, h->nx, h->ny, h->p.scene, h->p.lid_speed, h->p.inlet_speed);
-    if (ndisks > 0) k_raster_disks<<<(unsigned)ndisks, 256, 0, s>>>(h->d_info, h->nx, h->ny, d_disks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster_disks(lbm_handle* h, const double* d_disks, int ndisks, bool clear_state, cudaStream_t s) {
+    if (ndisks <= 0) return cudaSuccess;
+    k_raster_disks<<<(unsigned)ndisks, 256, 0, s>>>(
+        h->d_info, h->nx, h->ny, d_disks, clear_state ? (unsigned char*)h->buf[h->cur] : nullptr,
+        clear_state ? (unsigned char*)h->buf[h->cur ^ 1] : nullptr, (int)dtype_size(h->p.dtype), h->tiled, h->d_macro);
     return cudaGetLastError();
 }
 
